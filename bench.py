@@ -1,0 +1,432 @@
+#!/usr/bin/env python3
+"""Benchmark of the CellFlow simulation step on GB300.
+
+One bench step is one simulation step (cell list + force/density/integrator)
+of the configured workload, default the README-scale plain step: N=100,000
+particles, T=8 types, positions uniform in [-1,1]^3 (shifted to [0,2)^3),
+force table ~ N(0, 0.5), interaction radius 0.0920 (mean neighbour count
+about 40), dt 0.01.  Inputs are seeded synthetic data of that shape.
+
+Timing: W warm-up steps, then K steps each bracketed by CUDA events recorded
+on the library's stream around the step's phases (cf_profile_enable); a
+256 MiB write flushes L2 between timed steps, outside the timed intervals.
+value = N * K / (sum of step times), particle-steps/s.  e2e repeats the step
+through the public C ABI with host buffers: per step the AoS particle state
+(44 B per particle) goes host->device from pinned memory, the step runs, and
+the state comes back device->host; value = N * steps / host wall time.
+
+--impl reference times the reference's own step (its kernel body compiled on
+the host from its sources, oracle/_ref, with OpenMP on every core; the oracle
+restatement where that is absent) on a bounded sample of particles per step.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", default="plain_n100k_t8")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        rows = [r.split(",") for r in Path(self.path).read_text().splitlines() if r.strip()]
+        os.unlink(self.path)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, val in zip(names, r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_reference_sample(w, params, pos, types, table, radio, budget_s: float):
+    """Times the reference step on the host over a strided sample of rows.
+    Returns (particle-steps/s, kind, cores, sample description)."""
+    import numpy as np
+
+    import oracle
+
+    try:
+        oracle.build_ref(gpu=False)
+    except Exception:
+        pass
+    kind = "reference" if oracle.ref_available() else "port"
+    cores = os.cpu_count() or 1
+    vel = np.zeros_like(pos)
+    counts = np.zeros(w.n, np.int32)
+    rec = oracle.to_records(pos, vel, types)
+
+    def run(rows):
+        b, e, s = rows
+        t0 = time.perf_counter()
+        if kind == "reference":
+            oracle.ref_step(rec, table, radio, counts, params, rows=rows)
+        else:
+            oracle.step_f32(pos, vel, types, counts, table, radio, params, rows=rows)
+        return time.perf_counter() - t0, len(range(b, e, s))
+
+    # calibrate on a small sample, then size the sample to the budget
+    stride = max(1, w.n // (8 * cores))
+    dt, r = run((0, w.n, stride))
+    rate = r / max(dt, 1e-9)
+    rows_target = int(max(cores, min(w.n, rate * budget_s)))
+    stride = max(1, w.n // rows_target)
+    dt, r = run((0, w.n, stride))
+    desc = (f"{r} of {w.n} particles (every {stride}th), each against all {w.n}, one step from the initial "
+            f"state; {cores} OpenMP threads; {dt:.2f} s")
+    return r / dt, kind, cores, desc
+
+
+def run_reference_arm(args, rank, world):
+    """--impl reference: the reference's own step on the host cores."""
+    if rank != 0:
+        return
+    import numpy as np
+
+    from cellflow_gb300 import inputs
+
+    w = inputs.WORKLOADS[args.workload]
+    params = w.params()
+    pos, types, table = w.positions(), w.types(), w.table()
+    radio = np.zeros(w.num_types, np.float32)
+    import oracle
+
+    try:
+        oracle.build_ref(gpu=False)
+    except Exception:
+        pass
+    kind = "reference" if oracle.ref_available() else "port"
+    cores = os.cpu_count() or 1
+    vel = np.zeros_like(pos)
+    counts = np.zeros(w.n, np.int32)
+    rec = oracle.to_records(pos, vel, types)
+    # each step: a strided sample of rows sized to about one second
+    stride = max(1, w.n // (8 * cores))
+
+    def one(stride_):
+        rows = (0, w.n, stride_)
+        t0 = time.perf_counter()
+        if kind == "reference":
+            oracle.ref_step(rec, table, radio, counts, params, rows=rows)
+        else:
+            oracle.step_f32(pos, vel, types, counts, table, radio, params, rows=rows)
+        return time.perf_counter() - t0, len(range(*rows))
+
+    dt, r = one(stride)
+    stride = max(1, int(stride * dt / 1.0)) if dt > 0 else stride
+    for _ in range(args.warmup):
+        one(stride)
+    total_t, total_rows = 0.0, 0
+    for _ in range(args.steps):
+        dt, r = one(stride)
+        total_t += dt
+        total_rows += r
+    value = total_rows / total_t
+    sample = (f"per step {total_rows // max(args.steps, 1)} of {w.n} particles (every {stride}th), each against "
+              f"all {w.n}; {cores} OpenMP threads")
+    line = {
+        "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * w.n / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded Philox), see config",
+        "config": workload_config(w),
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(w) -> dict:
+    return {"workload": w.name, "n": w.n, "types": w.num_types, "radius": w.radius, "dt": w.delta_t,
+            "box": "[-1,1]^3 shifted to [0,2)^3", "positions": "uniform" if not w.blobs else
+            f"{w.blobs} gaussian blobs sigma {w.blob_sigma}", "force_table": f"N({w.table_mean},{w.table_sigma})",
+            "l2": "flushed between timed steps (256 MiB write)", "seed": w.seed}
+
+
+def run_gb300(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    import cellflow_gb300 as cf
+    from cellflow_gb300 import _lib, inputs
+    from cellflow_gb300.world import PARTICLE_DTYPE, ParticleSimulation
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = _lib.load()
+    w = inputs.WORKLOADS[args.workload]
+    params = w.params()
+    pos, types, table = w.positions(), w.types(), w.table()
+    radio = np.zeros(w.num_types, np.float32)
+    stream = torch.cuda.Stream()
+    sim = ParticleSimulation(w.n, w.num_types, w.extent, w.extent, w.extent)
+    sim.set_stream(stream.cuda_stream)
+    sim.set_particles(pos, types)
+    sim.setForceTable(table)
+    sim.setRadioByType(radio)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        sim.simulate(params, 1)
+    sim.sync()
+    state0 = sim.get_state()
+
+    # ---- timed region: K steps, per-phase CUDA events, L2 flushed between steps
+    _lib.check(lib.cf_profile_enable(sim.handle, 1), "cf_profile_enable")
+    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0])
+                          if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else local)
+    clocks.start()
+    barrier()
+    wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            flush.zero_()
+            sim.simulate(params, 1)
+    barrier()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    prof = _lib.PhaseTimes()
+    _lib.check(lib.cf_profile_read(sim.handle, C.byref(prof)), "cf_profile_read")
+    _lib.check(lib.cf_profile_enable(sim.handle, 0), "cf_profile_enable")
+    step_ms_total = prof.cell_list_ms + prof.force_ms
+    t_max = step_ms_total
+    if world > 1:
+        t = torch.tensor([step_ms_total], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = w.n * args.steps * world / (t_max * 1e-3)
+
+    # ---- work counters: replay the same K steps from the same state, untimed
+    sim.set_state(*state0)
+    c27_total, inter_total = 0, 0
+    for _ in range(args.steps):
+        c27, _ = sim.work_counters(params)
+        sim.simulate(params, 1)
+        _, inter = sim.work_counters(params)
+        c27_total += c27
+        inter_total += inter
+    flops = 9 * c27_total + 17 * inter_total + 25 * w.n * args.steps
+    force_s = prof.force_ms * 1e-3
+    achieved_tflops = flops / force_s / 1e12
+    peak_fp32 = C.c_double()
+    _lib.check(lib.cf_measure_fp32_peak(C.byref(peak_fp32)), "cf_measure_fp32_peak")
+    cells = 1
+    g = sim.grid(params)
+    for a in range(3):
+        cells *= g.cells[a]
+    cell_bytes = (112 * w.n + 8 * cells) * args.steps
+    cell_gbs = cell_bytes / (prof.cell_list_ms * 1e-3) / 1e9
+    peaks = measured_peaks()
+
+    # ---- end to end through the C ABI with host buffers
+    e2e_steps = args.e2e_steps or max(10, args.steps // 2)
+    host = torch.empty(w.n * PARTICLE_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+    host_np = host.numpy().view(PARTICLE_DTYPE)
+    sim.set_state(*state0)
+    host_np[:] = sim.getParticleData()
+    hp = C.c_void_p(host.data_ptr())
+    for _ in range(3):
+        _lib.check(lib.cf_set_particles(sim.handle, hp, w.n), "cf_set_particles")
+        sim.simulate(params, 1)
+        _lib.check(lib.cf_get_particles(sim.handle, hp, w.n), "cf_get_particles")
+    barrier()
+    e2e_wall = 0.0
+    for _ in range(e2e_steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _lib.check(lib.cf_set_particles(sim.handle, hp, w.n), "cf_set_particles")
+        sim.simulate(params, 1)
+        _lib.check(lib.cf_get_particles(sim.handle, hp, w.n), "cf_get_particles")
+        e2e_wall += time.perf_counter() - t0
+    e2e_value = w.n * e2e_steps * world / e2e_wall
+
+    # ---- reference kernel on this GPU (its O(N^2) kernel built for sm_103a), a few steps
+    ref_gpu = reference_gpu_kernel(w, params, pos, types, table, radio, stream) if rank == 0 else None
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            v, kind, cores, desc = cpu_reference_sample(w, params, pos, types, table, radio, args.cpu_seconds)
+            cpu = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": kind, "sample": desc}
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Philox4x32-10), shapes and distributions of the workload",
+            "config": workload_config(w),
+            "roofline": {
+                "kernel": "step_force_kernel (force + density + integrator)", "bound": "fp32",
+                "achieved": achieved_tflops, "peak": peak_fp32.value, "unit": "TFLOP/s",
+                "frac": achieved_tflops / peak_fp32.value,
+                "peak_source": "FP32 FMA chains on every SM, measured in this run (cf_measure_fp32_peak); "
+                               "MEASURED_PEAKS.json has no FP32 figure",
+                "work_model": "9*C27 + 17*I + 25*N flops per step",
+                "c27_per_particle_step": c27_total / (w.n * args.steps),
+                "interacting_per_particle_step": inter_total / (w.n * args.steps),
+                "traffic": None,
+            },
+            "roofline_cell_list": {
+                "bound": "hbm", "achieved": cell_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                "frac": cell_gbs / peaks.get("hbm_gbs", 6800.0),
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if not peaks.get("fallback") else "fallback",
+                "work_model": "112 B/particle + 8 B/cell per step",
+            },
+            "phase_ms_per_step": {"cell_list": prof.cell_list_ms / args.steps, "force": prof.force_ms / args.steps},
+            "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": w.n * 44,
+                    "d2h_bytes_per_step": w.n * 44, "steps": e2e_steps,
+                    "path": "cf_set_particles (pinned AoS) + cf_step + cf_get_particles"},
+            "gpu_launches": int(prof.launches),
+            "clocks": clk,
+            "wall_s_timed_region": wall,
+            "cpu_baseline": cpu,
+            "reference_gpu_kernel": ref_gpu,
+            "library": cf.__name__ + ": " + _lib.load().cf_version().decode(),
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def reference_gpu_kernel(w, params, pos, types, table, radio, stream):
+    """The reference step kernel (sm_103a build of ParticleSimulation.cu:69-166) on the same
+    inputs, launched as ParticleSimulation::simulate does; a few steps, CUDA events."""
+    import numpy as np
+    import torch
+
+    import oracle
+
+    try:
+        lib = oracle.ref_gpu_lib()
+    except (FileNotFoundError, OSError) as exc:
+        return {"unavailable": str(exc)}
+    rec = oracle.to_records(pos, np.zeros_like(pos), types)
+    d_part = torch.from_numpy(rec.view(np.uint8).copy()).cuda()
+    d_table = torch.from_numpy(np.ascontiguousarray(table, np.float32).ravel()).cuda()
+    d_radio = torch.from_numpy(radio).cuda()
+    cnt = [torch.zeros(w.n, dtype=torch.int32, device="cuda") for _ in range(2)]
+    p = params
+    steps = 3 if w.n <= 200_000 else 1
+
+    def launch(k):
+        rc = lib.cfref_gpu_step(C.c_void_p(d_part.data_ptr()), C.c_void_p(d_table.data_ptr()),
+                                C.c_void_p(d_radio.data_ptr()), C.c_void_p(cnt[k % 2].data_ptr()),
+                                C.c_void_p(cnt[(k + 1) % 2].data_ptr()), w.n, p.radius, p.delta_t, p.friction,
+                                p.repulsion, p.attraction, p.k, p.balance, p.canvas_width, p.canvas_height,
+                                p.canvas_depth, p.num_particle_types, p.ratio_with_lfo, p.force_multiplier,
+                                p.max_expected_neighbors, C.c_void_p(stream.cuda_stream))
+        if rc:
+            raise RuntimeError(f"reference kernel launch failed: {rc}")
+
+    with torch.cuda.stream(stream):
+        launch(0)
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(steps):
+            launch(k + 1)
+        e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": w.n / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms, "steps": steps,
+            "note": "reference O(N^2) kernel, in place (racy as in the reference), <<<ceil(N/256),256>>>"}
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+    run_gb300(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1047 @@
+// api.cpp - the C ABI (include/cellflow.h): world lifetime, parameter
+// surface, step driver, proximity graph and introspection.
+//
+// Host code of the reference this replaces: ParticleSimulation
+// (cuda-native/src/ParticleSimulation.cu:426-687).  Built with
+// -ffp-contract=off so the pair tables round exactly like the reference's
+// per-pair expressions (ParticleSimulation.cu:108-110, 521-531).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cf_internal.hpp"
+
+namespace cf {
+namespace {
+
+thread_local std::string g_error;
+
+constexpr int kMaxCells = 1 << 22;        // cap of the step and proximity grids
+constexpr int kMaxCanonicalCells = 1 << 24;  // cap of the work-model grid
+
+uint64_t splitmix64(uint64_t& s)
+{
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Uniform in [-1, 1), the range of the reference's rand()/RAND_MAX*2-1
+// (ParticleSimulation.cu:516, 535), from a seeded generator.
+float uniform_pm1(uint64_t& s)
+{
+    float u = (float)(splitmix64(s) >> 40) * (1.0f / 16777216.0f);
+    return u * 2.0f - 1.0f;
+}
+
+bool finite_positive(float v) { return std::isfinite(v) && v > 0.0f; }
+
+int check_world(const cf_world* w)
+{
+    if (!w) return fail(CF_ERR_INVALID, "null world");
+    return CF_OK;
+}
+
+template <typename T>
+cudaError_t dev_alloc(T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, sizeof(T) * count);
+}
+
+void dev_free(void* p)
+{
+    if (p) cudaFree(p);
+}
+
+void drop_graphs(cf_world* w)
+{
+    for (int k = 0; k < 2; k++) {
+        if (w->graph[k]) cudaGraphExecDestroy(w->graph[k]);
+        w->graph[k] = nullptr;
+        w->graph_bufs[k] = nullptr;
+    }
+}
+
+// (Re)allocate per-particle state and scratch for w->n particles.
+int alloc_particles(cf_world* w)
+{
+    const int n = w->n;
+    Scratch& s = w->s;
+    CF_CUDA(dev_alloc(&w->pos, n));
+    CF_CUDA(dev_alloc(&w->vel, n));
+    CF_CUDA(dev_alloc(&w->acc, n));
+    CF_CUDA(dev_alloc(&w->counts, n));
+    CF_CUDA(cudaMemsetAsync(w->counts, 0, sizeof(int) * (size_t)std::max(n, 1), w->stream));
+    for (int b = 0; b < 2; b++) {
+        CF_CUDA(dev_alloc(&s.keys[b], n));
+        CF_CUDA(dev_alloc(&s.vals[b], n));
+    }
+    CF_CUDA(dev_alloc(&s.pos_sorted, n));
+    s.hist_cap = radix_hist_entries(n);
+    CF_CUDA(dev_alloc(&s.hist, s.hist_cap));
+    s.scan_tmp_cap = std::max(scan_tmp_entries((int)s.hist_cap), scan_tmp_entries(n + 1));
+    CF_CUDA(dev_alloc(&s.scan_tmp, s.scan_tmp_cap));
+    CF_CUDA(dev_alloc(&s.counters, 2));
+    s.n_cap = n;
+    return CF_OK;
+}
+
+void free_particles(cf_world* w)
+{
+    drop_graphs(w);
+    Scratch& s = w->s;
+    dev_free(w->pos);
+    dev_free(w->vel);
+    dev_free(w->acc);
+    dev_free(w->counts);
+    for (int b = 0; b < 2; b++) {
+        dev_free(s.keys[b]);
+        dev_free(s.vals[b]);
+    }
+    dev_free(s.pos_sorted);
+    dev_free(s.hist);
+    dev_free(s.scan_tmp);
+    dev_free(s.cell_start);
+    dev_free(s.cell_end);
+    dev_free(s.prox_slots);
+    dev_free(s.prox_count);
+    dev_free(s.counters);
+    dev_free(s.cell_pop);
+    dev_free(w->aos);
+    w->pos = w->vel = w->acc = nullptr;
+    w->counts = nullptr;
+    w->aos = nullptr;
+    s = Scratch();
+}
+
+int ensure_cells(cf_world* w, int cells)
+{
+    Scratch& s = w->s;
+    if ((size_t)cells <= s.cells_cap) return CF_OK;
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    drop_graphs(w);
+    dev_free(s.cell_start);
+    dev_free(s.cell_end);
+    s.cell_start = s.cell_end = nullptr;
+    s.cells_cap = 0;
+    CF_CUDA(dev_alloc(&s.cell_start, cells));
+    CF_CUDA(dev_alloc(&s.cell_end, cells));
+    s.cells_cap = (size_t)cells;
+    return CF_OK;
+}
+
+int ensure_aos(cf_world* w)
+{
+    if (w->aos) return CF_OK;
+    CF_CUDA(dev_alloc(&w->aos, w->n));
+    return CF_OK;
+}
+
+int ensure_prox(cf_world* w)
+{
+    Scratch& s = w->s;
+    if (s.prox_slots) return CF_OK;
+    CF_CUDA(dev_alloc(&s.prox_slots, (size_t)w->n * CF_MAX_PROX_CONN));
+    CF_CUDA(dev_alloc(&s.prox_count, (size_t)w->n + 1));
+    return CF_OK;
+}
+
+// Wait for the world's stream and turn the device error word into a status.
+int sync_and_check(cf_world* w)
+{
+    int word = 0;
+    CF_CUDA(cudaMemcpyAsync(&word, w->err, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    if (word) {
+        CF_CUDA(cudaMemsetAsync(w->err, 0, sizeof(int), w->stream));
+        CF_CUDA(cudaStreamSynchronize(w->stream));
+        if (word & kDevErrWait) return fail(CF_ERR_DEVICE, "a bounded device wait gave up");
+        if (word & kDevErrType) return fail(CF_ERR_DOMAIN, "a particle type is outside [0, T)");
+        return fail(CF_ERR_DOMAIN, "a particle position is outside [0, extent) or not finite");
+    }
+    return CF_OK;
+}
+
+// Pair tables for a step (ParticleSimulation.cu:108-110, 116): effective
+// radius per type pair in the reference's float expression, the exact
+// sqrt threshold, and the force table; uploaded when anything changed.
+int update_pair_tables(cf_world* w, const cf_step_params* p, float* r_cut, int* uniform_r, float* eff_u,
+                       float* thr_u)
+{
+    const int T = w->num_types;
+    PairTables& h = w->host_tables;
+    bool changed = w->uploaded_version != w->table_version || w->uploaded_radius != p->radius ||
+                   w->uploaded_ratio != p->ratio_with_lfo || w->uploaded_types != T;
+    if (changed) {
+        std::fill(std::begin(h.force), std::end(h.force), 0.0f);
+        std::fill(std::begin(h.eff), std::end(h.eff), 0.0f);
+        std::fill(std::begin(h.threshold), std::end(h.threshold), 0.0f);
+        for (int a = 0; a < T; a++) {
+            for (int b = 0; b < T; b++) {
+                const float ra = p->radius * (1.0f + w->radio[a] * p->ratio_with_lfo);
+                const float rb = p->radius * (1.0f + w->radio[b] * p->ratio_with_lfo);
+                const float eff = (ra + rb) * 0.5f;
+                const int k = a * kTableStride + b;
+                h.force[k] = w->table[a * T + b];
+                h.eff[k] = eff;
+                h.threshold[k] = sqrt_threshold(eff);
+            }
+        }
+        CF_CUDA(cudaMemcpyAsync(w->tables, &h, sizeof(PairTables), cudaMemcpyHostToDevice, w->stream));
+        w->uploaded_version = w->table_version;
+        w->uploaded_radius = p->radius;
+        w->uploaded_ratio = p->ratio_with_lfo;
+        w->uploaded_types = T;
+    }
+    float thr_max = 0.0f;
+    bool uniform = true;
+    const uint32_t* eff_bits = reinterpret_cast<const uint32_t*>(h.eff);
+    for (int a = 0; a < T; a++)
+        for (int b = 0; b < T; b++) {
+            const int k = a * kTableStride + b;
+            thr_max = std::max(thr_max, h.threshold[k]);
+            uniform = uniform && eff_bits[k] == eff_bits[0];
+        }
+    *r_cut = cutoff_distance(thr_max);
+    *uniform_r = uniform ? 1 : 0;
+    *eff_u = h.eff[0];
+    *thr_u = h.threshold[0];
+    return CF_OK;
+}
+
+int check_params(const cf_world* w, const cf_step_params* p)
+{
+    if (!p) return fail(CF_ERR_INVALID, "null step parameters");
+    if (p->num_particle_types != w->num_types)
+        return fail(CF_ERR_INVALID, "num_particle_types differs from the world's type count");
+    if (!finite_positive(p->canvas_width) || !finite_positive(p->canvas_height) || !finite_positive(p->canvas_depth))
+        return fail(CF_ERR_INVALID, "canvas extents must be finite and positive");
+    if (!std::isfinite(p->radius)) return fail(CF_ERR_INVALID, "radius must be finite");
+    return CF_OK;
+}
+
+// Host-side cell list: hash, stable radix sort, start/end and sorted snapshot.
+// Returns the buffer index that holds the sorted keys and values.
+int build_cell_list(cf_world* w, const Grid& g, const float* ext, int* which)
+{
+    Scratch& s = w->s;
+    int rc = ensure_cells(w, g.cells);
+    if (rc) return rc;
+    CF_CUDA(launch_cell_hash(w->pos, w->n, g, ext, w->num_types, s.keys[0], w->err, w->stream));
+    CF_CUDA(launch_radix_sort(s, w->n, g.key_bits, which, w->stream));
+    CF_CUDA(launch_cell_bounds(s.keys[*which], s.vals[*which], w->n, w->pos, s.cell_start, s.cell_end, g.cells,
+                               s.pos_sorted, w->stream));
+    return CF_OK;
+}
+
+int prepare_step(cf_world* w, const cf_step_params* p, StepConsts* c)
+{
+    int rc = check_params(w, p);
+    if (rc) return rc;
+    float r_cut = 0.0f;
+    std::memset(c, 0, sizeof(*c));
+    rc = update_pair_tables(w, p, &r_cut, &c->uniform_r, &c->eff_uniform, &c->thr_uniform);
+    if (rc) return rc;
+    c->ext[0] = p->canvas_width;
+    c->ext[1] = p->canvas_height;
+    c->ext[2] = p->canvas_depth;
+    for (int a = 0; a < 3; a++) c->half[a] = c->ext[a] * 0.5f;
+    c->grid = choose_step_grid(c->ext, r_cut, kMaxCells);
+    c->n = w->n;
+    c->num_types = w->num_types;
+    c->repulsion = p->repulsion;
+    c->attraction = p->attraction;
+    c->neg_k = -p->k;
+    c->balance = p->balance;
+    c->force_multiplier = p->force_multiplier;
+    c->delta_t = p->delta_t;
+    c->friction = p->friction;
+    c->max_expected_neighbors = p->max_expected_neighbors;
+    return CF_OK;
+}
+
+// One step's launches on the world's stream: cell list, then the fused force,
+// density and integrator kernel; with the three profiling events when prof.
+int enqueue_step(cf_world* w, const StepConsts& c, int prof)
+{
+    if (prof) CF_CUDA(cudaEventRecord(w->prof_ev[0], w->stream));
+    int which = 0;
+    int rc = build_cell_list(w, c.grid, c.ext, &which);
+    if (rc) return rc;
+    if (prof) CF_CUDA(cudaEventRecord(w->prof_ev[1], w->stream));
+    CF_CUDA(launch_step_force(c, w->tables, w->s.pos_sorted, w->s.keys[which], w->s.vals[which], w->s.cell_start,
+                              w->s.cell_end, w->pos, w->vel, w->acc, w->counts, w->stream));
+    if (prof) CF_CUDA(cudaEventRecord(w->prof_ev[2], w->stream));
+    return CF_OK;
+}
+
+// The one-step graph for these constants, captured on first use and again
+// whenever the constants or the scratch buffers change.
+int step_graph(cf_world* w, const StepConsts& c, int prof, cudaGraphExec_t* out)
+{
+    const void* bufs = w->s.cell_start;
+    if (w->graph[prof] && w->graph_bufs[prof] == bufs && std::memcmp(&w->graph_key[prof], &c, sizeof(c)) == 0) {
+        *out = w->graph[prof];
+        return CF_OK;
+    }
+    if (w->graph[prof]) {
+        cudaGraphExecDestroy(w->graph[prof]);
+        w->graph[prof] = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    CF_CUDA(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_step(w, c, prof);
+    cudaError_t e = cudaStreamEndCapture(w->stream, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&w->graph[prof], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    w->graph_key[prof] = c;
+    w->graph_bufs[prof] = bufs;
+    *out = w->graph[prof];
+    return CF_OK;
+}
+
+int respawn(cf_world* w, uint64_t seed, float spawn_region)
+{
+    float lo[3], span[3];
+    for (int a = 0; a < 3; a++) {
+        span[a] = std::min(spawn_region, w->ext[a]);
+        lo[a] = (w->ext[a] - span[a]) * 0.5f;
+    }
+    CF_CUDA(launch_init_particles(w->pos, w->vel, w->acc, w->counts, w->n, w->num_types, lo, span, seed, w->stream));
+    return CF_OK;
+}
+
+void seed_tables(cf_world* w, uint64_t seed)
+{
+    uint64_t s = seed ^ 0xC3A5C85C97CB3127ull;
+    const int T = w->num_types;
+    for (int i = 0; i < T * T; i++) w->raw[i] = uniform_pm1(s);
+    for (int i = 0; i < T; i++) w->radio[i] = uniform_pm1(s);
+}
+
+void transform_table(cf_world* w, float range, float bias, float offset)
+{
+    // ParticleSimulation.cu:524-527, tanh on a float resolves to tanhf
+    const int T = w->num_types;
+    for (int i = 0; i < T * T; i++) {
+        const float t = tanhf(w->raw[i] * offset) * range + bias;
+        w->table[i] = fmaxf(-1.0f, fminf(1.0f, t));
+    }
+    w->table_version++;
+}
+
+}  // namespace
+
+int fail(int code, const std::string& msg)
+{
+    g_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    g_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? CF_ERR_ALLOC : CF_ERR_CUDA;
+}
+
+// Smallest float t >= 0 with sqrtf(t) >= eff.  sqrtf is monotone, so for
+// every s: sqrtf(s) < eff  <=>  s < t.
+float sqrt_threshold(float eff)
+{
+    if (!(eff > 0.0f)) return 0.0f;
+    if (std::isinf(eff)) return INFINITY;
+    float t = eff * eff;
+    if (std::isinf(t)) t = FLT_MAX;
+    while (t > 0.0f && sqrtf(t) >= eff) t = nextafterf(t, 0.0f);
+    while (sqrtf(t) < eff) {
+        t = nextafterf(t, INFINITY);
+        if (std::isinf(t)) break;
+    }
+    return t;
+}
+
+// Largest true distance a pair can have and still pass fl(d^2 + 1e-4) < t,
+// with slack for the rounding of the displacement, the squares and sums.
+float cutoff_distance(float threshold)
+{
+    if (std::isinf(threshold)) return INFINITY;
+    double t = (double)threshold * (1.0 + 0x1p-22) - 0.0001 * (1.0 - 0x1p-22);
+    if (!(t > 0.0)) return 0.0f;
+    return (float)(std::sqrt(t / (1.0 - 0x1p-20)) * (1.0 + 0x1p-20));
+}
+
+namespace {
+
+// Cells per axis for a cutoff: the largest m whose cell side exceeds the
+// cutoff by the hash rounding slack (cell coordinates are computed as
+// fl(x * fl(m / L)), off by at most m * 2^-23 cells).
+int cells_for_cutoff(double extent, double cut)
+{
+    if (!(cut > 0.0) || !std::isfinite(cut)) return cut > 0.0 ? 1 : 4096;
+    double m = std::floor(extent / cut);
+    if (m > 4096) m = 4096;
+    if (m < 1) m = 1;
+    int mi = (int)m;
+    while (mi > 1 && extent / mi < cut / (1.0 - 4.0 * mi * 0x1p-23) * (1.0 + 0x1p-20)) mi--;
+    return mi;
+}
+
+void finish_grid(Grid& g, const float* ext, int max_cells)
+{
+    // cap the total by coarsening the finest axis
+    while ((long long)g.m[0] * g.m[1] * g.m[2] > max_cells) {
+        int a = 0;
+        for (int b = 1; b < 3; b++)
+            if (g.m[b] > g.m[a]) a = b;
+        g.m[a] = std::max(1, g.m[a] * 3 / 4);
+    }
+    if (g.periodic) {
+        g.generic = 0;
+        for (int a = 0; a < 3; a++)
+            if (g.m[a] < 5) g.generic = 1;
+        if (g.generic)
+            for (int a = 0; a < 3; a++)
+                if (g.m[a] < 3) g.m[a] = 1;
+    }
+    for (int a = 0; a < 3; a++) g.inv[a] = (float)((double)g.m[a] / (double)ext[a]);
+    g.cells = g.m[0] * g.m[1] * g.m[2];
+    g.key_bits = 0;
+    while ((1ll << g.key_bits) < (long long)g.cells) g.key_bits++;
+}
+
+}  // namespace
+
+Grid choose_step_grid(const float* ext, float r_cut, int max_cells)
+{
+    Grid g;
+    std::memset(&g, 0, sizeof(g));
+    g.periodic = 1;
+    for (int a = 0; a < 3; a++) g.m[a] = cells_for_cutoff(ext[a], r_cut);
+    finish_grid(g, ext, max_cells);
+    return g;
+}
+
+Grid choose_prox_grid(const float* ext, float distance, int max_cells)
+{
+    Grid g;
+    std::memset(&g, 0, sizeof(g));
+    g.periodic = 0;
+    double dsq = (double)(distance * distance);
+    double cut = std::sqrt(dsq * (1.0 + 0x1p-22) / (1.0 - 0x1p-20)) * (1.0 + 0x1p-20);
+    for (int a = 0; a < 3; a++) g.m[a] = distance > 0.0f ? cells_for_cutoff(ext[a], cut) : 1;
+    finish_grid(g, ext, max_cells);
+    return g;
+}
+
+// The work model's grid: floor(L / r_max) cells per axis of side L / cells.
+Grid canonical_grid(const float* ext, float r_max)
+{
+    Grid g;
+    std::memset(&g, 0, sizeof(g));
+    g.periodic = 1;
+    for (int a = 0; a < 3; a++) {
+        double m = r_max > 0.0f ? std::floor((double)ext[a] / (double)r_max) : 1.0;
+        g.m[a] = (int)std::min(std::max(m, 1.0), 4096.0);
+    }
+    while ((long long)g.m[0] * g.m[1] * g.m[2] > kMaxCanonicalCells) {
+        int a = 0;
+        for (int b = 1; b < 3; b++)
+            if (g.m[b] > g.m[a]) a = b;
+        g.m[a] = std::max(1, g.m[a] * 3 / 4);
+    }
+    for (int a = 0; a < 3; a++) g.inv[a] = (float)((double)g.m[a] / (double)ext[a]);
+    g.cells = g.m[0] * g.m[1] * g.m[2];
+    return g;
+}
+
+}  // namespace cf
+
+using namespace cf;
+
+extern "C" {
+
+const char* cf_last_error(void) { return g_error.c_str(); }
+
+const char* cf_version(void) { return "cellflow-gb300 0.1 (sm_103a)"; }
+
+void cf_default_params(cf_step_params* p)
+{
+    if (!p) return;
+    // SimulationParams.h:15-29
+    p->radius = 42.07f;
+    p->delta_t = 0.18f;
+    p->friction = 0.51f;
+    p->repulsion = 64.83f;
+    p->attraction = 3.06f;
+    p->k = 29.45f;
+    p->balance = 0.79f;
+    p->canvas_width = 8000.0f;
+    p->canvas_height = 8000.0f;
+    p->canvas_depth = 8000.0f;
+    p->num_particle_types = 6;
+    p->ratio_with_lfo = 0.0f;
+    p->force_multiplier = 2.33f;
+    p->max_expected_neighbors = 400;
+}
+
+int cf_create(int n, int num_types, float w_, float h_, float d_, uint64_t seed, cf_world** out)
+{
+    if (!out) return fail(CF_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (n < 0) return fail(CF_ERR_INVALID, "particle count must be >= 0");
+    if (num_types < 1 || num_types > CF_MAX_TYPES) return fail(CF_ERR_INVALID, "type count must be in [1, 32]");
+    if (!finite_positive(w_) || !finite_positive(h_) || !finite_positive(d_))
+        return fail(CF_ERR_INVALID, "box extents must be finite and positive");
+    cf_world* w = new cf_world();
+    w->n = n;
+    w->num_types = num_types;
+    w->ext[0] = w_;
+    w->ext[1] = h_;
+    w->ext[2] = d_;
+    std::memset(w->raw, 0, sizeof(w->raw));
+    std::memset(w->table, 0, sizeof(w->table));
+    std::memset(w->radio, 0, sizeof(w->radio));
+    auto bail = [&](int rc) {
+        cf_destroy(w);
+        return rc;
+    };
+    cudaError_t e = cudaGetDevice(&w->device);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaGetDevice"));
+    e = cudaStreamCreateWithFlags(&w->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreateWithFlags"));
+    w->stream = w->own_stream;
+    e = dev_alloc(&w->err, 1);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(error word)"));
+    e = cudaMemsetAsync(w->err, 0, sizeof(int), w->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemsetAsync"));
+    e = dev_alloc(&w->tables, 1);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(tables)"));
+    int rc = alloc_particles(w);
+    if (rc) return bail(rc);
+    // ParticleSimulation.cu:430-434: particles, force table (0.28, -0.20, 1.0), radius table
+    seed_tables(w, seed);
+    transform_table(w, 0.28f, -0.20f, 1.0f);
+    rc = respawn(w, seed, 2000.0f);
+    if (rc) return bail(rc);
+    rc = sync_and_check(w);
+    if (rc) return bail(rc);
+    *out = w;
+    return CF_OK;
+}
+
+int cf_destroy(cf_world* w)
+{
+    if (!w) return CF_OK;
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    for (int k = 0; k < 3; k++)
+        if (w->prof_ev[k]) cudaEventDestroy(w->prof_ev[k]);
+    drop_graphs(w);
+    free_particles(w);
+    dev_free(w->err);
+    dev_free(w->tables);
+    if (w->own_stream) cudaStreamDestroy(w->own_stream);
+    delete w;
+    return CF_OK;
+}
+
+int cf_set_stream(cf_world* w, void* stream)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    w->stream = stream ? (cudaStream_t)stream : w->own_stream;
+    return CF_OK;
+}
+
+int cf_sync(cf_world* w)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    return sync_and_check(w);
+}
+
+int cf_particle_count(const cf_world* w, int* n)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!n) return fail(CF_ERR_INVALID, "null output");
+    *n = w->n;
+    return CF_OK;
+}
+
+int cf_num_particle_types(const cf_world* w, int* t)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!t) return fail(CF_ERR_INVALID, "null output");
+    *t = w->num_types;
+    return CF_OK;
+}
+
+int cf_set_particle_count(cf_world* w, int n, uint64_t seed)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (n < 0) return fail(CF_ERR_INVALID, "particle count must be >= 0");
+    if (n == w->n) return CF_OK;  // ParticleSimulation.cu:565
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    free_particles(w);
+    w->n = n;
+    rc = alloc_particles(w);
+    if (rc) return rc;
+    rc = respawn(w, seed, 2000.0f);
+    if (rc) return rc;
+    return sync_and_check(w);
+}
+
+int cf_set_num_particle_types(cf_world* w, int t, uint64_t seed)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (t < 1 || t > CF_MAX_TYPES) return fail(CF_ERR_INVALID, "type count must be in [1, 32]");
+    w->num_types = t;  // ParticleSimulation.cu:575-578
+    seed_tables(w, seed);
+    transform_table(w, 0.28f, -0.20f, 1.0f);
+    rc = respawn(w, seed, 2000.0f);
+    if (rc) return rc;
+    return sync_and_check(w);
+}
+
+int cf_initialize_particles(cf_world* w, uint64_t seed, float spawn_region)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!(spawn_region > 0.0f)) return fail(CF_ERR_INVALID, "spawn region must be positive");
+    rc = respawn(w, seed, spawn_region);
+    if (rc) return rc;
+    return sync_and_check(w);
+}
+
+int cf_get_particles(cf_world* w, cf_particle* out, int n)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (n != w->n || (!out && n > 0)) return fail(CF_ERR_INVALID, "output must hold exactly n particles");
+    rc = ensure_aos(w);
+    if (rc) return rc;
+    CF_CUDA(launch_soa_to_aos(w->pos, w->vel, w->acc, w->aos, n, w->stream));
+    if (n > 0)
+        CF_CUDA(cudaMemcpyAsync(out, w->aos, sizeof(cf_particle) * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    return sync_and_check(w);
+}
+
+int cf_set_particles(cf_world* w, const cf_particle* in, int n)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (n != w->n || (!in && n > 0)) return fail(CF_ERR_INVALID, "input must hold exactly n particles");
+    rc = ensure_aos(w);
+    if (rc) return rc;
+    if (n > 0)
+        CF_CUDA(cudaMemcpyAsync(w->aos, in, sizeof(cf_particle) * (size_t)n, cudaMemcpyHostToDevice, w->stream));
+    CF_CUDA(launch_aos_to_soa(w->aos, w->pos, w->vel, w->acc, n, w->stream));
+    return CF_OK;
+}
+
+int cf_get_state(cf_world* w, float* pos4, float* vel4, int* counts)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    const size_t n = (size_t)w->n;
+    if (n > 0) {
+        if (pos4) CF_CUDA(cudaMemcpyAsync(pos4, w->pos, 16 * n, cudaMemcpyDeviceToHost, w->stream));
+        if (vel4) CF_CUDA(cudaMemcpyAsync(vel4, w->vel, 16 * n, cudaMemcpyDeviceToHost, w->stream));
+        if (counts) CF_CUDA(cudaMemcpyAsync(counts, w->counts, 4 * n, cudaMemcpyDeviceToHost, w->stream));
+    }
+    return sync_and_check(w);
+}
+
+int cf_set_state(cf_world* w, const float* pos4, const float* vel4, const int* counts)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    const size_t n = (size_t)w->n;
+    if (n > 0) {
+        if (pos4) CF_CUDA(cudaMemcpyAsync(w->pos, pos4, 16 * n, cudaMemcpyHostToDevice, w->stream));
+        if (vel4) CF_CUDA(cudaMemcpyAsync(w->vel, vel4, 16 * n, cudaMemcpyHostToDevice, w->stream));
+        if (counts) CF_CUDA(cudaMemcpyAsync(w->counts, counts, 4 * n, cudaMemcpyHostToDevice, w->stream));
+    }
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    return CF_OK;
+}
+
+int cf_get_neighbor_counts(cf_world* w, int* out, int n)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (n != w->n || (!out && n > 0)) return fail(CF_ERR_INVALID, "output must hold exactly n counts");
+    if (n > 0) CF_CUDA(cudaMemcpyAsync(out, w->counts, 4 * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
+    return sync_and_check(w);
+}
+
+int cf_device_buffers(cf_world* w, cf_device_view* out)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!out) return fail(CF_ERR_INVALID, "null output");
+    out->pos4 = w->pos;
+    out->vel4 = w->vel;
+    out->acc4 = w->acc;
+    out->counts = w->counts;
+    out->n = w->n;
+    return CF_OK;
+}
+
+int cf_get_raw_force_table(cf_world* w, float* raw, int count)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!raw || count != w->num_types * w->num_types) return fail(CF_ERR_INVALID, "count must be T*T");
+    std::memcpy(raw, w->raw, sizeof(float) * count);
+    return CF_OK;
+}
+
+int cf_set_raw_force_table(cf_world* w, const float* raw, int count)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!raw || count != w->num_types * w->num_types) return fail(CF_ERR_INVALID, "count must be T*T");
+    std::memcpy(w->raw, raw, sizeof(float) * count);
+    return CF_OK;
+}
+
+int cf_regenerate_force_table(cf_world* w, uint64_t seed)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    // ParticleSimulation.cu:513-519: new raw values, then (0.28, -0.20, 1.0)
+    uint64_t s = seed ^ 0x2545F4914F6CDD1Dull;
+    for (int i = 0; i < w->num_types * w->num_types; i++) w->raw[i] = uniform_pm1(s);
+    transform_table(w, 0.28f, -0.20f, 1.0f);
+    return CF_OK;
+}
+
+int cf_update_force_table(cf_world* w, float range, float bias, float offset)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    transform_table(w, range, bias, offset);
+    return CF_OK;
+}
+
+int cf_set_force_table(cf_world* w, const float* table, int count)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!table || count != w->num_types * w->num_types) return fail(CF_ERR_INVALID, "count must be T*T");
+    std::memcpy(w->table, table, sizeof(float) * count);
+    w->table_version++;
+    return CF_OK;
+}
+
+int cf_get_force_table(cf_world* w, float* table, int count)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!table || count != w->num_types * w->num_types) return fail(CF_ERR_INVALID, "count must be T*T");
+    std::memcpy(table, w->table, sizeof(float) * count);
+    return CF_OK;
+}
+
+int cf_get_radio_by_type(cf_world* w, float* out, int count)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!out || count != w->num_types) return fail(CF_ERR_INVALID, "count must be T");
+    std::memcpy(out, w->radio, sizeof(float) * count);
+    return CF_OK;
+}
+
+int cf_set_radio_by_type(cf_world* w, const float* values, int count)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!values || count != w->num_types) return fail(CF_ERR_INVALID, "count must be T");
+    std::memcpy(w->radio, values, sizeof(float) * count);
+    w->table_version++;
+    return CF_OK;
+}
+
+int cf_set_radio_by_type_value(cf_world* w, int index, float value)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    // ParticleSimulation.cu:615-622: out-of-range indices are ignored
+    if (index >= 0 && index < w->num_types) {
+        w->radio[index] = value;
+        w->table_version++;
+    }
+    return CF_OK;
+}
+
+int cf_rotate_radio_by_type(cf_world* w)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    // ParticleSimulation.cu:594-600
+    const int T = w->num_types;
+    const float last = w->radio[T - 1];
+    for (int i = T - 1; i > 0; i--) w->radio[i] = w->radio[i - 1];
+    w->radio[0] = last;
+    w->table_version++;
+    return CF_OK;
+}
+
+float cf_lfo_ratio(float ratio, float lfo_a, float lfo_s, float t_seconds)
+{
+    // CellFlowWidget.cpp:414-421
+    if (lfo_a != 0.0f) {
+        const float lfo = (float)(lfo_a * std::sin(2.0f * M_PI * lfo_s * t_seconds));
+        return ratio + lfo;
+    }
+    return ratio;
+}
+
+int cf_step(cf_world* w, const cf_step_params* p, int nsteps)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (nsteps < 0) return fail(CF_ERR_INVALID, "nsteps must be >= 0");
+    StepConsts c;
+    rc = prepare_step(w, p, &c);
+    if (rc) return rc;
+    rc = ensure_cells(w, c.grid.cells);
+    if (rc) return rc;
+    const int prof = w->profiling ? 1 : 0;
+    cudaGraphExec_t exec = nullptr;
+    if (w->use_graphs && w->stream != nullptr && nsteps > 0) {
+        rc = step_graph(w, c, prof, &exec);
+        if (rc) return rc;
+    }
+    const long long launches = cell_list_launches(w->n, c.grid.key_bits) + (w->n > 0 ? 1 : 0);
+    for (int s = 0; s < nsteps; s++) {
+        if (exec)
+            CF_CUDA(cudaGraphLaunch(exec, w->stream));
+        else {
+            rc = enqueue_step(w, c, prof);
+            if (rc) return rc;
+        }
+        if (prof) {
+            // serialised steps: read this step's phase times
+            CF_CUDA(cudaEventSynchronize(w->prof_ev[2]));
+            float a = 0.0f, b = 0.0f;
+            CF_CUDA(cudaEventElapsedTime(&a, w->prof_ev[0], w->prof_ev[1]));
+            CF_CUDA(cudaEventElapsedTime(&b, w->prof_ev[1], w->prof_ev[2]));
+            w->prof_cell_ms += a;
+            w->prof_force_ms += b;
+            w->prof_steps++;
+            w->prof_launches += launches;
+        }
+    }
+    return CF_OK;
+}
+
+int cf_profile_enable(cf_world* w, int on)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    for (int k = 0; k < 3; k++)
+        if (!w->prof_ev[k]) CF_CUDA(cudaEventCreate(&w->prof_ev[k]));
+    w->profiling = on != 0;
+    w->prof_cell_ms = w->prof_force_ms = 0.0;
+    w->prof_steps = w->prof_launches = 0;
+    return CF_OK;
+}
+
+int cf_profile_read(cf_world* w, cf_phase_times* out)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!out) return fail(CF_ERR_INVALID, "null output");
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    out->cell_list_ms = w->prof_cell_ms;
+    out->force_ms = w->prof_force_ms;
+    out->steps = w->prof_steps;
+    out->launches = w->prof_launches;
+    w->prof_cell_ms = w->prof_force_ms = 0.0;
+    w->prof_steps = w->prof_launches = 0;
+    return CF_OK;
+}
+
+int cf_get_grid(cf_world* w, const cf_step_params* p, cf_grid_info* out)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!out) return fail(CF_ERR_INVALID, "null output");
+    StepConsts c;
+    rc = prepare_step(w, p, &c);
+    if (rc) return rc;
+    for (int a = 0; a < 3; a++) {
+        out->cells[a] = c.grid.m[a];
+        out->inv_cell[a] = c.grid.inv[a];
+    }
+    float r_max = 0.0f;
+    for (int a = 0; a < w->num_types; a++)
+        for (int b = 0; b < w->num_types; b++) r_max = std::max(r_max, w->host_tables.eff[a * kTableStride + b]);
+    out->r_max = r_max;
+    out->generic_wrap = c.grid.generic;
+    out->key_bits = c.grid.key_bits;
+    return CF_OK;
+}
+
+int cf_debug_cell_list(cf_world* w, const cf_step_params* p, uint32_t* cell_of, uint32_t* sorted_idx,
+                       uint32_t* cell_start, uint32_t* cell_end, int cells_cap)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    StepConsts c;
+    rc = prepare_step(w, p, &c);
+    if (rc) return rc;
+    if (cells_cap < c.grid.cells) return fail(CF_ERR_CAPACITY, "cell arrays smaller than the grid");
+    int which = 0;
+    rc = build_cell_list(w, c.grid, c.ext, &which);
+    if (rc) return rc;
+    // the hash wrote cell ids in original order into keys[0] before sorting;
+    // recompute them (the sort may have reused that buffer)
+    CF_CUDA(launch_cell_hash(w->pos, w->n, c.grid, c.ext, w->num_types, w->s.keys[which ^ 1], w->err, w->stream));
+    const size_t n = (size_t)w->n;
+    if (n > 0) {
+        if (cell_of) CF_CUDA(cudaMemcpyAsync(cell_of, w->s.keys[which ^ 1], 4 * n, cudaMemcpyDeviceToHost, w->stream));
+        if (sorted_idx)
+            CF_CUDA(cudaMemcpyAsync(sorted_idx, w->s.vals[which], 4 * n, cudaMemcpyDeviceToHost, w->stream));
+    }
+    if (cell_start)
+        CF_CUDA(cudaMemcpyAsync(cell_start, w->s.cell_start, 4 * (size_t)c.grid.cells, cudaMemcpyDeviceToHost,
+                                w->stream));
+    if (cell_end)
+        CF_CUDA(
+            cudaMemcpyAsync(cell_end, w->s.cell_end, 4 * (size_t)c.grid.cells, cudaMemcpyDeviceToHost, w->stream));
+    return sync_and_check(w);
+}
+
+int cf_work_counters(cf_world* w, const cf_step_params* p, uint64_t* c27, uint64_t* interacting)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    StepConsts c;
+    rc = prepare_step(w, p, &c);
+    if (rc) return rc;
+    float r_max = 0.0f;
+    for (int a = 0; a < w->num_types; a++)
+        for (int b = 0; b < w->num_types; b++) r_max = std::max(r_max, w->host_tables.eff[a * kTableStride + b]);
+    Grid g = canonical_grid(c.ext, r_max);
+    Scratch& s = w->s;
+    if ((size_t)g.cells > s.pop_cap) {
+        CF_CUDA(cudaStreamSynchronize(w->stream));
+        dev_free(s.cell_pop);
+        s.cell_pop = nullptr;
+        s.pop_cap = 0;
+        CF_CUDA(dev_alloc(&s.cell_pop, g.cells));
+        s.pop_cap = (size_t)g.cells;
+    }
+    CF_CUDA(launch_work_counters(w->pos, w->counts, w->n, g, s.cell_pop, s.counters, w->stream));
+    unsigned long long host[2] = {0, 0};
+    CF_CUDA(cudaMemcpyAsync(host, s.counters, sizeof(host), cudaMemcpyDeviceToHost, w->stream));
+    rc = sync_and_check(w);
+    if (rc) return rc;
+    if (c27) *c27 = host[0];
+    if (interacting) *interacting = host[1];
+    return CF_OK;
+}
+
+namespace {
+
+// Proximity selection: cell list with the proximity grid, per-particle
+// edges, exclusive scan.  Leaves offsets in prox_count[0..n].
+int proximity_prepare(cf_world* w, float distance, int max_conn, uint32_t* total)
+{
+    if (!(distance >= 0.0f) || !std::isfinite(distance)) return fail(CF_ERR_INVALID, "distance must be finite, >= 0");
+    if (max_conn < 0 || max_conn > CF_MAX_PROX_CONN)
+        return fail(CF_ERR_INVALID, "max_conn must be in [0, 16] (the reference overflowed its buffer above 16)");
+    int rc = ensure_prox(w);
+    if (rc) return rc;
+    Grid g = choose_prox_grid(w->ext, distance, kMaxCells);
+    int which = 0;
+    rc = build_cell_list(w, g, w->ext, &which);
+    if (rc) return rc;
+    Scratch& s = w->s;
+    const float dsq = distance * distance;  // ParticleSimulation.cu:660
+    CF_CUDA(cudaMemsetAsync(s.prox_count + w->n, 0, sizeof(uint32_t), w->stream));
+    CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_start, s.cell_end, g, w->n,
+                                    dsq, max_conn, s.prox_slots, s.prox_count, w->stream));
+    CF_CUDA(launch_scan_exclusive(s.prox_count, s.prox_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
+    CF_CUDA(cudaMemcpyAsync(total, s.prox_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    return sync_and_check(w);
+}
+
+}  // namespace
+
+int cf_proximity_edges(cf_world* w, float distance, int max_conn, int32_t* edges, int cap, int* n_edges)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (cap < 0 || (cap > 0 && !edges)) return fail(CF_ERR_INVALID, "bad edge buffer");
+    uint32_t total = 0;
+    rc = proximity_prepare(w, distance, max_conn, &total);
+    if (rc) return rc;
+    if (n_edges) *n_edges = (int)total;
+    const int write = (int)std::min<uint32_t>(total, (uint32_t)cap);
+    if (write > 0) {
+        int32_t* d_edges = nullptr;
+        CF_CUDA(dev_alloc(&d_edges, 2 * (size_t)write));
+        cudaError_t e = launch_proximity_emit_edges(w->s.prox_slots, w->s.prox_count, w->n, max_conn, d_edges, write,
+                                                    w->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(edges, d_edges, 8 * (size_t)write, cudaMemcpyDeviceToHost, w->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
+        cudaFree(d_edges);
+        if (e != cudaSuccess) return cuda_fail(e, "proximity edges");
+    }
+    if (total > (uint32_t)cap) return fail(CF_ERR_CAPACITY, "edge buffer smaller than the edge count");
+    return CF_OK;
+}
+
+int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, const cf_color* colors, int n_colors,
+                                 float* vertices, int cap_vertices, int* vertex_count)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!colors || n_colors < w->num_types) return fail(CF_ERR_INVALID, "need one colour per type");
+    if (cap_vertices < 0 || (cap_vertices > 0 && !vertices)) return fail(CF_ERR_INVALID, "bad vertex buffer");
+    uint32_t total = 0;
+    rc = proximity_prepare(w, distance, max_conn, &total);
+    if (rc) return rc;
+    if (vertex_count) *vertex_count = (int)(2 * total);
+    if (total > 0 && cap_vertices > 0) {
+        float* d_colors = nullptr;
+        CF_CUDA(dev_alloc(&d_colors, 3 * (size_t)w->num_types));
+        // ParticleSimulation.cu:253 indexes colours by type % numParticleTypes
+        cudaError_t e = cudaMemcpyAsync(d_colors, colors, sizeof(float) * 3 * w->num_types, cudaMemcpyHostToDevice,
+                                        w->stream);
+        if (e == cudaSuccess)
+            e = launch_proximity_emit_vertices(w->s.prox_slots, w->s.prox_count, w->n, max_conn, w->pos, d_colors,
+                                               w->num_types, vertices, cap_vertices, w->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
+        cudaFree(d_colors);
+        if (e != cudaSuccess) return cuda_fail(e, "proximity vertices");
+    }
+    if (2 * (size_t)total > (size_t)cap_vertices) return fail(CF_ERR_CAPACITY, "vertex buffer too small");
+    return CF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,394 @@
+// celllist.cu - uniform-grid cell list: cell hash, stable LSD radix sort,
+// cell start/end with the sorted position snapshot, device-wide scan, and
+// the work-model counters.
+//
+// The reference has no spatial structure (its step is O(N^2),
+// cuda-native/src/ParticleSimulation.cu:86); this list is what makes a step
+// O(N * neighbours).  Its order is fixed: particles sorted by cell id with
+// ties in index order, the result a stable sort gives, so the order and every
+// per-cell range are reproducible bit for bit.
+#include <cuda_runtime.h>
+
+#include "cf_internal.hpp"
+
+namespace cf {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kRadix = 256;
+constexpr int kWarps = kThreads / 32;
+
+__device__ __forceinline__ int cell_coord(float x, float inv, int m)
+{
+    int c = __float2int_rd(__fmul_rn(x, inv));
+    return min(max(c, 0), m - 1);
+}
+
+// Cell id of every particle; flags positions outside [0, extent) or not
+// finite, and types outside [0, T).
+__global__ void __launch_bounds__(kThreads)
+    cell_hash_kernel(const float4* __restrict__ pos, int n, Grid g, float ex, float ey, float ez, int num_types,
+                     uint32_t* __restrict__ keys, int* __restrict__ err)
+{
+    int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos[i];
+    bool inside = (p.x >= 0.0f && p.x < ex) && (p.y >= 0.0f && p.y < ey) && (p.z >= 0.0f && p.z < ez);
+    if (!inside) atomicOr(err, kDevErrDomain);
+    if (__float_as_uint(p.w) >= (uint32_t)num_types) atomicOr(err, kDevErrType);
+    int cx = cell_coord(p.x, g.inv[0], g.m[0]);
+    int cy = cell_coord(p.y, g.inv[1], g.m[1]);
+    int cz = cell_coord(p.z, g.inv[2], g.m[2]);
+    keys[i] = (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
+}
+
+// Digit histogram of one tile of kThreads*ITEMS keys, written digit-major:
+// hist[digit * nblocks + block].
+template <int ITEMS>
+__global__ void __launch_bounds__(kThreads)
+    radix_hist_kernel(const uint32_t* __restrict__ keys, int n, int shift, uint32_t* __restrict__ hist, int nblocks)
+{
+    __shared__ uint32_t h[kRadix];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int base = blockIdx.x * (kThreads * ITEMS);
+#pragma unroll
+    for (int it = 0; it < ITEMS; it++) {
+        int i = base + it * kThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & (kRadix - 1)], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter of one tile.  Keys are visited in index order, kThreads at a
+// time; within a round a key's rank among equal digits is the count of equal
+// digits in lower lanes (__match_any_sync), in lower warps (shared counts),
+// and in earlier rounds (running offsets).  vals_in == nullptr means the
+// identity permutation (first pass).
+template <int ITEMS>
+__global__ void __launch_bounds__(kThreads)
+    radix_scatter_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                         uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int n, int shift,
+                         const uint32_t* __restrict__ offsets, int nblocks)
+{
+    __shared__ uint32_t running[kRadix];
+    __shared__ uint32_t warp_cnt[kWarps][kRadix];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    running[tid] = offsets[tid * nblocks + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) warp_cnt[w][tid] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * (kThreads * ITEMS);
+    for (int it = 0; it < ITEMS; it++) {
+        int i = base + it * kThreads + tid;
+        bool valid = i < n;
+        uint32_t key = valid ? keys_in[i] : 0u;
+        uint32_t val = valid ? (vals_in ? vals_in[i] : (uint32_t)i) : 0u;
+        uint32_t digit = valid ? ((key >> shift) & (kRadix - 1)) : (uint32_t)(kRadix + lane);
+        uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        uint32_t lower = peers & ((1u << lane) - 1u);
+        if (valid && lower == 0u) warp_cnt[warp][digit] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t dst = running[digit] + __popc(lower);
+            for (int w = 0; w < warp; w++) dst += warp_cnt[w][digit];
+            keys_out[dst] = key;
+            vals_out[dst] = val;
+        }
+        __syncthreads();
+        uint32_t add = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; w++) {
+            add += warp_cnt[w][tid];
+            warp_cnt[w][tid] = 0;
+        }
+        running[tid] += add;
+        __syncthreads();
+    }
+}
+
+// ---- device-wide exclusive scan (three phases) -----------------------------
+
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total)
+{
+    __shared__ uint32_t warp_sums[kWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t s = lane < kWarps ? warp_sums[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < kWarps; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < kWarps) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    uint32_t before = warp ? warp_sums[warp - 1] : 0u;
+    *total = warp_sums[kWarps - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(kThreads) scan_tile_sums(const uint32_t* __restrict__ in, int n, uint32_t* sums)
+{
+    int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
+        if (base + k < n) s += in[base + k];
+    uint32_t total;
+    block_exclusive_scan(s, &total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of count values in one block, in place.
+__global__ void __launch_bounds__(kThreads) scan_single_block(uint32_t* data, int count)
+{
+    uint32_t carry = 0;
+    for (int base = 0; base < count; base += kScanTile) {
+        int idx = base + threadIdx.x * kScanItems;
+        uint32_t v[kScanItems];
+        uint32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            v[k] = idx + k < count ? data[idx + k] : 0u;
+            s += v[k];
+        }
+        uint32_t total;
+        uint32_t run = carry + block_exclusive_scan(s, &total);
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            if (idx + k < count) data[idx + k] = run;
+            run += v[k];
+        }
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    scan_apply(const uint32_t* in, uint32_t* out, int n, const uint32_t* __restrict__ sums)
+{
+    int idx = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        v[k] = idx + k < n ? in[idx + k] : 0u;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t run = sums[blockIdx.x] + block_exclusive_scan(s, &total);
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (idx + k < n) out[idx + k] = run;
+        run += v[k];
+    }
+}
+
+// Cell start/end from the sorted keys, and the snapshot of positions in
+// sorted order.  Empty cells keep the 0/0 written before the launch.
+__global__ void __launch_bounds__(kThreads)
+    cell_bounds_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, int n,
+                       const float4* __restrict__ pos, uint32_t* __restrict__ start, uint32_t* __restrict__ end,
+                       float4* __restrict__ pos_sorted)
+{
+    int t = blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n) return;
+    uint32_t k = keys[t];
+    if (t == 0 || keys[t - 1] != k) start[k] = (uint32_t)t;
+    if (t == n - 1 || keys[t + 1] != k) end[k] = (uint32_t)(t + 1);
+    pos_sorted[t] = pos[vals[t]];
+}
+
+// ---- work counters ---------------------------------------------------------
+
+__device__ __forceinline__ uint32_t canon_cell(float4 p, const Grid& g)
+{
+    int cx = cell_coord(p.x, g.inv[0], g.m[0]);
+    int cy = cell_coord(p.y, g.inv[1], g.m[1]);
+    int cz = cell_coord(p.z, g.inv[2], g.m[2]);
+    return (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
+}
+
+__global__ void __launch_bounds__(kThreads)
+    population_kernel(const float4* __restrict__ pos, int n, Grid g, uint32_t* __restrict__ pop)
+{
+    int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i < n) atomicAdd(&pop[canon_cell(pos[i], g)], 1u);
+}
+
+// Distinct stencil coordinates along one periodic axis.
+__device__ __forceinline__ int stencil_axis(int c, int m, int* out)
+{
+    int k = 0;
+    for (int o = -1; o <= 1; o++) {
+        int v = c + o;
+        v = v < 0 ? v + m : (v >= m ? v - m : v);
+        bool dup = false;
+        for (int q = 0; q < k; q++) dup |= out[q] == v;
+        if (!dup) out[k++] = v;
+    }
+    return k;
+}
+
+__global__ void __launch_bounds__(kThreads)
+    c27_kernel(const float4* __restrict__ pos, const int* __restrict__ counts, int n, Grid g,
+               const uint32_t* __restrict__ pop, unsigned long long* __restrict__ out)
+{
+    int i = blockIdx.x * kThreads + threadIdx.x;
+    unsigned long long cand = 0, inter = 0;
+    if (i < n) {
+        uint32_t c = canon_cell(pos[i], g);
+        int cx = (int)(c % (uint32_t)g.m[0]);
+        int cy = (int)((c / (uint32_t)g.m[0]) % (uint32_t)g.m[1]);
+        int cz = (int)(c / (uint32_t)(g.m[0] * g.m[1]));
+        int ox[3], oy[3], oz[3];
+        int nx = stencil_axis(cx, g.m[0], ox), ny = stencil_axis(cy, g.m[1], oy), nz = stencil_axis(cz, g.m[2], oz);
+        for (int a = 0; a < nz; a++)
+            for (int b = 0; b < ny; b++)
+                for (int e = 0; e < nx; e++) cand += pop[(oz[a] * g.m[1] + oy[b]) * g.m[0] + ox[e]];
+        cand -= 1;
+        inter = (unsigned long long)counts[i];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cand += __shfl_down_sync(0xffffffffu, cand, o);
+        inter += __shfl_down_sync(0xffffffffu, inter, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&out[0], cand);
+        atomicAdd(&out[1], inter);
+    }
+}
+
+inline int blocks_for(int n, int per_block) { return (n + per_block - 1) / per_block; }
+
+constexpr int kSortItemsSmall = 4;
+constexpr int kSortItemsLarge = 16;
+
+inline int sort_items(int n) { return n <= (1 << 18) ? kSortItemsSmall : kSortItemsLarge; }
+
+}  // namespace
+
+size_t radix_hist_entries(int n)
+{
+    int items = sort_items(n);
+    size_t nblocks = (size_t)blocks_for(n > 0 ? n : 1, kThreads * items);
+    return nblocks * kRadix;
+}
+
+size_t scan_tmp_entries(int n) { return (size_t)blocks_for(n > 0 ? n : 1, kScanTile) + 1; }
+
+// Kernel launches of one cell-list build: hash, per radix pass histogram +
+// scan (1 or 3 kernels) + scatter, and start/end.
+int cell_list_launches(int n, int key_bits)
+{
+    if (n <= 0) return 0;
+    int passes = (key_bits + 7) / 8;
+    if (passes < 1) passes = 1;
+    int entries = (int)radix_hist_entries(n);
+    int scan = blocks_for(entries, kScanTile) == 1 ? 1 : 3;
+    return 1 + passes * (2 + scan) + 1;
+}
+
+cudaError_t launch_cell_hash(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
+                             uint32_t* keys, int* err, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    cell_hash_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(pos, n, g, ext[0], ext[1], ext[2], num_types,
+                                                                  keys, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_exclusive(const uint32_t* in, uint32_t* out, int n, uint32_t* tmp, size_t tmp_cap,
+                                  cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    int tiles = blocks_for(n, kScanTile);
+    if ((size_t)tiles > tmp_cap) return cudaErrorInvalidValue;
+    if (tiles == 1) {
+        if (in != out) {
+            cudaError_t e = cudaMemcpyAsync(out, in, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+        scan_single_block<<<1, kThreads, 0, st>>>(out, n);
+        return cudaGetLastError();
+    }
+    scan_tile_sums<<<tiles, kThreads, 0, st>>>(in, n, tmp);
+    scan_single_block<<<1, kThreads, 0, st>>>(tmp, tiles);
+    scan_apply<<<tiles, kThreads, 0, st>>>(in, out, n, tmp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_radix_sort(Scratch& s, int n, int key_bits, int* which, cudaStream_t st)
+{
+    *which = 0;
+    if (n <= 0) return cudaSuccess;
+    int items = sort_items(n);
+    int nblocks = blocks_for(n, kThreads * items);
+    int passes = (key_bits + 7) / 8;
+    if (passes < 1) passes = 1;
+    size_t entries = (size_t)nblocks * kRadix;
+    if (entries > s.hist_cap) return cudaErrorInvalidValue;
+    int cur = 0;
+    for (int p = 0; p < passes; p++) {
+        int shift = 8 * p;
+        const uint32_t* vals_in = p == 0 ? nullptr : s.vals[cur];
+        if (items == kSortItemsSmall)
+            radix_hist_kernel<kSortItemsSmall><<<nblocks, kThreads, 0, st>>>(s.keys[cur], n, shift, s.hist, nblocks);
+        else
+            radix_hist_kernel<kSortItemsLarge><<<nblocks, kThreads, 0, st>>>(s.keys[cur], n, shift, s.hist, nblocks);
+        cudaError_t e = launch_scan_exclusive(s.hist, s.hist, (int)entries, s.scan_tmp, s.scan_tmp_cap, st);
+        if (e != cudaSuccess) return e;
+        if (items == kSortItemsSmall)
+            radix_scatter_kernel<kSortItemsSmall><<<nblocks, kThreads, 0, st>>>(
+                s.keys[cur], vals_in, s.keys[cur ^ 1], s.vals[cur ^ 1], n, shift, s.hist, nblocks);
+        else
+            radix_scatter_kernel<kSortItemsLarge><<<nblocks, kThreads, 0, st>>>(
+                s.keys[cur], vals_in, s.keys[cur ^ 1], s.vals[cur ^ 1], n, shift, s.hist, nblocks);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        cur ^= 1;
+    }
+    *which = cur;
+    return cudaSuccess;
+}
+
+cudaError_t launch_cell_bounds(const uint32_t* keys, const uint32_t* vals, int n, const float4* pos, uint32_t* start,
+                               uint32_t* end, int cells, float4* pos_sorted, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(start, 0, sizeof(uint32_t) * (size_t)cells, st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(end, 0, sizeof(uint32_t) * (size_t)cells, st);
+    if (e != cudaSuccess) return e;
+    if (n <= 0) return cudaSuccess;
+    cell_bounds_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(keys, vals, n, pos, start, end, pos_sorted);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_work_counters(const float4* pos, const int* counts, int n, const Grid& canon, uint32_t* pop,
+                                 unsigned long long* out, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(pop, 0, sizeof(uint32_t) * (size_t)canon.cells, st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    if (n <= 0) return cudaSuccess;
+    population_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(pos, n, canon, pop);
+    c27_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(pos, counts, n, canon, pop, out);
+    return cudaGetLastError();
+}
+
+}  // namespace cf

@@ -1,0 +1,179 @@
+// cf_internal.hpp - shared declarations of the CellFlow GB300 library.
+//
+// Device data layout (all in HBM, original particle order unless noted):
+//   pos4[n]   float4 x, y, z, type (uint32 bits)    16 B/particle
+//   vel4[n]   float4 vx, vy, vz, 0                   16 B/particle
+//   acc4[n]   float4 ax, ay, az, 0                   16 B/particle
+//   counts[n] int32 neighbour counts (read as "previous", rewritten)
+// Per-step scratch (cell list, sorted order):
+//   keys/vals  uint32 cell id and particle index, two buffers each (radix
+//              sort ping-pong); pos_sorted float4[n] snapshot in cell order;
+//   cell_start/cell_end uint32[cells]; radix histograms.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/cellflow.h"
+
+namespace cf {
+
+// Device error word bits (kernels atomicOr them; the host reads at sync).
+enum : int {
+    kDevErrDomain = 1,  // a position outside [0, extent) or not finite
+    kDevErrType = 2,    // a type outside [0, T)
+    kDevErrWait = 4,    // a bounded device wait gave up
+};
+
+// Tables padded to the maximum type count so any 5-bit type index stays in
+// bounds: index = (self & 31) * 32 + (other & 31).
+constexpr int kTableStride = CF_MAX_TYPES;
+constexpr int kTableSize = CF_MAX_TYPES * CF_MAX_TYPES;
+
+// Per-pair tables for a step, uploaded together.
+struct PairTables {
+    float force[kTableSize];      // F[self][other]
+    float eff[kTableSize];        // effective radius (ParticleSimulation.cu:108-110)
+    float threshold[kTableSize];  // smallest float t with sqrtf(t) >= eff
+};
+
+// Grid of one cell list.
+struct Grid {
+    int m[3];         // cells per axis
+    float inv[3];     // hash multipliers, float(m / extent)
+    int cells;        // m0 * m1 * m2
+    int key_bits;     // bits of a cell id
+    int generic;      // 1: full reference wrap per candidate (some axis < 5 cells)
+    int periodic;     // 1: periodic stencil (step), 0: clipped (proximity)
+};
+
+// Everything the step kernels read besides the buffers.
+struct StepConsts {
+    float ext[3];      // W, H, D
+    float half[3];     // W*0.5f, ...
+    Grid grid;
+    int n;
+    int num_types;
+    int uniform_r;     // all pairs share one effective radius
+    float eff_uniform;
+    float thr_uniform;
+    float repulsion, attraction, neg_k, balance, force_multiplier, delta_t, friction;
+    int max_expected_neighbors;
+};
+
+struct Scratch {
+    uint32_t* keys[2] = {nullptr, nullptr};
+    uint32_t* vals[2] = {nullptr, nullptr};
+    uint32_t* hist = nullptr;       // radix digit histograms / scan partials
+    size_t hist_cap = 0;            // entries
+    uint32_t* cell_start = nullptr;
+    uint32_t* cell_end = nullptr;
+    size_t cells_cap = 0;
+    float4* pos_sorted = nullptr;
+    int n_cap = 0;
+    // proximity
+    int32_t* prox_slots = nullptr;  // n * CF_MAX_PROX_CONN partner indices
+    uint32_t* prox_count = nullptr; // n + 1 (exclusive-scanned in place)
+    uint32_t* scan_tmp = nullptr;   // block partials of the device-wide scan
+    size_t scan_tmp_cap = 0;
+    // work counters
+    unsigned long long* counters = nullptr;  // [0] C27, [1] I
+    uint32_t* cell_pop = nullptr;            // canonical-grid populations
+    size_t pop_cap = 0;
+};
+
+}  // namespace cf
+
+struct cf_world {
+    int device = 0;
+    int n = 0;
+    int num_types = 0;
+    float ext[3] = {0, 0, 0};
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    float4* pos = nullptr;
+    float4* vel = nullptr;
+    float4* acc = nullptr;
+    int* counts = nullptr;
+    cf_particle* aos = nullptr;  // staging for AoS transfers (allocated on first use)
+    int* err = nullptr;          // device error word
+    cf::PairTables* tables = nullptr;
+    cf::Scratch s;
+    // host-side parameter surface
+    float raw[cf::kTableSize];
+    float table[cf::kTableSize];
+    float radio[CF_MAX_TYPES];
+    uint64_t table_version = 1;
+    // cache of the uploaded pair tables
+    uint64_t uploaded_version = 0;
+    float uploaded_radius = -1.0f;
+    float uploaded_ratio = 0.0f;
+    int uploaded_types = -1;
+    cf::PairTables host_tables;
+    // phase profiling (cf_profile_enable): events start / after cell list / after force
+    bool profiling = false;
+    cudaEvent_t prof_ev[3] = {nullptr, nullptr, nullptr};
+    double prof_cell_ms = 0.0, prof_force_ms = 0.0;
+    long long prof_steps = 0, prof_launches = 0;
+    // one-step CUDA graphs (index 1: with the profiling events), re-captured
+    // when the step constants or buffers change
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cf::StepConsts graph_key[2];
+    const void* graph_bufs[2] = {nullptr, nullptr};
+    bool use_graphs = true;
+};
+
+namespace cf {
+
+// Error plumbing (thread-local message, see cf_last_error).
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+#define CF_CUDA(call)                                                   \
+    do {                                                                \
+        cudaError_t cf_e_ = (call);                                     \
+        if (cf_e_ != cudaSuccess) return ::cf::cuda_fail(cf_e_, #call); \
+    } while (0)
+
+// Launchers (return a CUDA error code; called with the world's stream).
+cudaError_t launch_cell_hash(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
+                             uint32_t* keys, int* err, cudaStream_t st);
+cudaError_t launch_radix_sort(Scratch& s, int n, int key_bits, int* which, cudaStream_t st);
+cudaError_t launch_cell_bounds(const uint32_t* keys, const uint32_t* vals, int n, const float4* pos, uint32_t* start,
+                               uint32_t* end, int cells, float4* pos_sorted, cudaStream_t st);
+cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
+                              const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_start,
+                              const uint32_t* cell_end, float4* pos, float4* vel, float4* acc, int* counts,
+                              cudaStream_t st);
+cudaError_t launch_scan_exclusive(const uint32_t* in, uint32_t* out, int n, uint32_t* tmp, size_t tmp_cap,
+                                  cudaStream_t st);
+size_t scan_tmp_entries(int n);
+size_t radix_hist_entries(int n);
+int cell_list_launches(int n, int key_bits);
+cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* keys_sorted,
+                                    const uint32_t* vals_sorted, const uint32_t* cell_start,
+                                    const uint32_t* cell_end, const Grid& g, int n, float dsq, int max_conn,
+                                    int32_t* slots, uint32_t* count, cudaStream_t st);
+cudaError_t launch_proximity_emit_edges(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,
+                                        int32_t* edges, int cap, cudaStream_t st);
+cudaError_t launch_proximity_emit_vertices(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,
+                                           const float4* pos, const float* colors, int n_colors, float* vertices,
+                                           int cap_vertices, cudaStream_t st);
+cudaError_t launch_init_particles(float4* pos, float4* vel, float4* acc, int* counts, int n, int num_types,
+                                  const float* lo, const float* span, uint64_t seed, cudaStream_t st);
+cudaError_t launch_aos_to_soa(const cf_particle* aos, float4* pos, float4* vel, float4* acc, int n, cudaStream_t st);
+cudaError_t launch_soa_to_aos(const float4* pos, const float4* vel, const float4* acc, cf_particle* aos, int n,
+                              cudaStream_t st);
+cudaError_t launch_work_counters(const float4* pos, const int* counts, int n, const Grid& canon, uint32_t* pop,
+                                 unsigned long long* out, cudaStream_t st);
+
+// Host helpers (api.cpp).
+Grid choose_step_grid(const float* ext, float r_cut, int max_cells);
+Grid choose_prox_grid(const float* ext, float distance, int max_cells);
+Grid canonical_grid(const float* ext, float r_max);
+float sqrt_threshold(float eff);
+float cutoff_distance(float threshold);
+
+}  // namespace cf

@@ -1,0 +1,65 @@
+// peak.cu - FP32 FMA throughput probe, the denominator of the force
+// kernel's roofline.  Every thread runs 8 independent FMA chains so the
+// FMA pipe, not latency, limits it; the grid covers every SM several times.
+#include <cuda_runtime.h>
+
+#include "cf_internal.hpp"
+
+namespace cf {
+namespace {
+
+constexpr int kChains = 8;
+constexpr int kIters = 4096;
+constexpr int kThreads = 256;
+
+__global__ void __launch_bounds__(kThreads) fma_chains_kernel(float* out, float a, float b)
+{
+    float v[kChains];
+#pragma unroll
+    for (int c = 0; c < kChains; c++) v[c] = threadIdx.x * 1e-3f + c;
+    for (int it = 0; it < kIters; it++) {
+#pragma unroll
+        for (int c = 0; c < kChains; c++) v[c] = fmaf(v[c], a, b);
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int c = 0; c < kChains; c++) s += v[c];
+    if (s == 1234.5f) out[blockIdx.x] = s;  // keeps the chains live
+}
+
+}  // namespace
+}  // namespace cf
+
+extern "C" int cf_measure_fp32_peak(double* tflops)
+{
+    using namespace cf;
+    if (!tflops) return fail(CF_ERR_INVALID, "null output");
+    int dev = 0, sms = 0;
+    CF_CUDA(cudaGetDevice(&dev));
+    CF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    float* out = nullptr;
+    const int blocks = sms * 8;
+    CF_CUDA(cudaMalloc(&out, sizeof(float) * blocks));
+    cudaStream_t st;
+    CF_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1;
+    CF_CUDA(cudaEventCreate(&e0));
+    CF_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 6; rep++) {
+        CF_CUDA(cudaEventRecord(e0, st));
+        fma_chains_kernel<<<blocks, kThreads, 0, st>>>(out, 0.999999f, 1e-7f);
+        CF_CUDA(cudaEventRecord(e1, st));
+        CF_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        CF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    cudaFree(out);
+    const double flops = 2.0 * kChains * (double)kIters * kThreads * blocks;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return CF_OK;
+}

@@ -1,0 +1,170 @@
+// proximity.cu - proximity-graph edges on the cell list.
+//
+// The reference kernel (cuda-native/src/ParticleSimulation.cu:188-277) scans
+// j = i+1 .. N-1 in index order, keeps same-type particles with non-periodic
+// squared distance below distance^2 until it holds 2*maxConn of them
+// (:215), insertion-sorts them by squared distance (:235-243, stable) and
+// emits the first maxConn (:246-275) through an atomicAdd offset (:250).
+//
+// Here each particle scans only the cells within the distance and keeps the
+// 2*maxConn smallest qualifying indices, which is the same candidate set;
+// the same stable sort by squared distance then picks the same edges.  Edges
+// are placed by an exclusive scan of per-particle counts, so the output order
+// is deterministic: by i, then by distance.
+#include <cuda_runtime.h>
+
+#include "cf_internal.hpp"
+
+namespace cf {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kMaxHeld = 2 * CF_MAX_PROX_CONN;
+
+__global__ void __launch_bounds__(kThreads)
+    proximity_select_kernel(const float4* __restrict__ pos_sorted, const uint32_t* __restrict__ keys_sorted,
+                            const uint32_t* __restrict__ vals_sorted, const uint32_t* __restrict__ cell_start,
+                            const uint32_t* __restrict__ cell_end, Grid g, int n, float dsq, int max_conn,
+                            int32_t* __restrict__ slots, uint32_t* __restrict__ count)
+{
+    const int t = blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n) return;
+    const float4 h = pos_sorted[t];
+    const uint32_t i = vals_sorted[t];
+    const uint32_t key = keys_sorted[t];
+    const int mx = g.m[0], my = g.m[1], mz = g.m[2];
+    const int cx = (int)(key % (uint32_t)mx);
+    const int cy = (int)((key / (uint32_t)mx) % (uint32_t)my);
+    const int cz = (int)(key / (uint32_t)(mx * my));
+    const int cap = 2 * max_conn;
+    if (cap <= 0) {
+        count[i] = 0;
+        return;
+    }
+
+    int held = 0;
+    int hj[kMaxHeld];
+    float hd[kMaxHeld];
+    for (int z = max(cz - 1, 0); z <= min(cz + 1, mz - 1); z++) {
+        for (int y = max(cy - 1, 0); y <= min(cy + 1, my - 1); y++) {
+            for (int x = max(cx - 1, 0); x <= min(cx + 1, mx - 1); x++) {
+                const uint32_t cell = (uint32_t)((z * my + y) * mx + x);
+                const uint32_t u_end = cell_end[cell];
+                for (uint32_t u = cell_start[cell]; u < u_end; u++) {
+                    const float4 q = pos_sorted[u];
+                    if (__float_as_uint(q.w) != __float_as_uint(h.w)) continue;
+                    const int j = (int)vals_sorted[u];
+                    if (j <= (int)i) continue;
+                    if (held == cap && j >= hj[cap - 1]) continue;
+                    const float dx = __fsub_rn(q.x, h.x);
+                    const float dy = __fsub_rn(q.y, h.y);
+                    const float dz = __fsub_rn(q.z, h.z);
+                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    if (!(d2 < dsq)) continue;
+                    // insert into the index-ordered set, dropping the largest when full
+                    int p = held < cap ? held : cap - 1;
+                    while (p > 0 && hj[p - 1] > j) {
+                        hj[p] = hj[p - 1];
+                        hd[p] = hd[p - 1];
+                        p--;
+                    }
+                    hj[p] = j;
+                    hd[p] = d2;
+                    if (held < cap) held++;
+                }
+            }
+        }
+    }
+    // stable insertion sort by squared distance (ParticleSimulation.cu:235-243)
+    for (int a = 1; a < held; a++) {
+        const float kd = hd[a];
+        const int kj = hj[a];
+        int b = a - 1;
+        while (b >= 0 && hd[b] > kd) {
+            hd[b + 1] = hd[b];
+            hj[b + 1] = hj[b];
+            b--;
+        }
+        hd[b + 1] = kd;
+        hj[b + 1] = kj;
+    }
+    const int emit = held < max_conn ? held : max_conn;
+    for (int e = 0; e < emit; e++) slots[(size_t)i * CF_MAX_PROX_CONN + e] = hj[e];
+    count[i] = (uint32_t)emit;
+}
+
+__global__ void __launch_bounds__(256)
+    proximity_edges_kernel(const int32_t* __restrict__ slots, const uint32_t* __restrict__ offsets, int n,
+                           int32_t* __restrict__ edges, int cap)
+{
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = offsets[i], e_count = offsets[i + 1] - o;
+    for (uint32_t e = 0; e < e_count; e++) {
+        const uint32_t k = o + e;
+        if (k < (uint32_t)cap) {
+            edges[2 * (size_t)k] = i;
+            edges[2 * (size_t)k + 1] = slots[(size_t)i * CF_MAX_PROX_CONN + e];
+        }
+    }
+}
+
+// Line vertices in the reference's layout (ParticleSimulation.cu:253-275):
+// per edge, vertex of i then vertex of j, each x, y, z, r, g, b with the
+// colour of i's type.
+__global__ void __launch_bounds__(256)
+    proximity_vertices_kernel(const int32_t* __restrict__ slots, const uint32_t* __restrict__ offsets, int n,
+                              const float4* __restrict__ pos, const float* __restrict__ colors, int n_colors,
+                              float* __restrict__ vertices, int cap_vertices)
+{
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = offsets[i], e_count = offsets[i + 1] - o;
+    if (e_count == 0) return;
+    const float4 a = pos[i];
+    const uint32_t c = __float_as_uint(a.w) % (uint32_t)n_colors;
+    const float r = colors[3 * c], gg = colors[3 * c + 1], b = colors[3 * c + 2];
+    for (uint32_t e = 0; e < e_count; e++) {
+        const uint32_t k = o + e;
+        if (2 * (size_t)k + 1 >= (size_t)cap_vertices) break;
+        const float4 q = pos[slots[(size_t)i * CF_MAX_PROX_CONN + e]];
+        float* v = vertices + (size_t)k * 12;
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = r; v[4] = gg; v[5] = b;
+        v[6] = q.x; v[7] = q.y; v[8] = q.z; v[9] = r; v[10] = gg; v[11] = b;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* keys_sorted,
+                                    const uint32_t* vals_sorted, const uint32_t* cell_start,
+                                    const uint32_t* cell_end, const Grid& g, int n, float dsq, int max_conn,
+                                    int32_t* slots, uint32_t* count, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    proximity_select_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+        pos_sorted, keys_sorted, vals_sorted, cell_start, cell_end, g, n, dsq, max_conn, slots, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_proximity_emit_edges(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,
+                                        int32_t* edges, int cap, cudaStream_t st)
+{
+    (void)max_conn;
+    if (n <= 0 || cap <= 0) return cudaSuccess;
+    proximity_edges_kernel<<<(n + 255) / 256, 256, 0, st>>>(slots, offsets, n, edges, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_proximity_emit_vertices(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,
+                                           const float4* pos, const float* colors, int n_colors, float* vertices,
+                                           int cap_vertices, cudaStream_t st)
+{
+    (void)max_conn;
+    if (n <= 0 || cap_vertices <= 0) return cudaSuccess;
+    proximity_vertices_kernel<<<(n + 255) / 256, 256, 0, st>>>(slots, offsets, n, pos, colors, n_colors, vertices,
+                                                               cap_vertices);
+    return cudaGetLastError();
+}
+
+}  // namespace cf

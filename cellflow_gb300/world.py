@@ -1,0 +1,268 @@
+"""Python mirror of the reference's ``ParticleSimulation`` over the C ABI.
+
+Method names follow cuda-native/include/ParticleSimulation.cuh:10-103 so
+tests and tools read like code written against the reference class; every
+call goes through libcellflow.so.  Arrays are numpy; a failing call raises
+``CellFlowError`` (the reference printed and exited instead).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, fields
+
+import numpy as np
+
+from . import _lib
+from ._lib import Color, DeviceView, GridInfo, Particle, StepParams, check, load
+
+PARTICLE_DTYPE = np.dtype(
+    [("pos", "<f4", 3), ("vel", "<f4", 3), ("acc", "<f4", 3), ("ptype", "<u4"), ("pad", "<f4")]
+)
+assert PARTICLE_DTYPE.itemsize == 44
+
+
+@dataclass
+class SimulationParams:
+    """Physics subset of the reference SimulationParams (SimulationParams.h:15-29)."""
+
+    radius: float = 42.07
+    delta_t: float = 0.18
+    friction: float = 0.51
+    repulsion: float = 64.83
+    attraction: float = 3.06
+    k: float = 29.45
+    balance: float = 0.79
+    canvas_width: float = 8000.0
+    canvas_height: float = 8000.0
+    canvas_depth: float = 8000.0
+    num_particle_types: int = 6
+    ratio_with_lfo: float = 0.0
+    force_multiplier: float = 2.33
+    max_expected_neighbors: int = 400
+
+    def to_c(self) -> StepParams:
+        p = StepParams()
+        for f in fields(self):
+            setattr(p, f.name, getattr(self, f.name))
+        return p
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class ParticleSimulation:
+    """One world: n particles of T types in a W x H x D periodic box."""
+
+    def __init__(self, n: int, num_types: int = 6, width: float = 8000.0, height: float = 8000.0,
+                 depth: float | None = None, seed: int = 1):
+        lib = load()
+        self._lib = lib
+        self._h = C.c_void_p()
+        depth = height if depth is None else depth  # ParticleSimulation.cu:439 uses height for depth
+        check(lib.cf_create(n, num_types, width, height, depth, seed, C.byref(self._h)), "cf_create")
+
+    # ---- lifetime -----------------------------------------------------------
+    def close(self) -> None:
+        if self._h:
+            self._lib.cf_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def getParticleCount(self) -> int:
+        n = C.c_int()
+        check(self._lib.cf_particle_count(self._h, C.byref(n)), "cf_particle_count")
+        return n.value
+
+    def getNumParticleTypes(self) -> int:
+        t = C.c_int()
+        check(self._lib.cf_num_particle_types(self._h, C.byref(t)), "cf_num_particle_types")
+        return t.value
+
+    def setParticleCount(self, n: int, seed: int = 1) -> None:
+        check(self._lib.cf_set_particle_count(self._h, n, seed), "cf_set_particle_count")
+
+    def setNumParticleTypes(self, t: int, seed: int = 1) -> None:
+        check(self._lib.cf_set_num_particle_types(self._h, t, seed), "cf_set_num_particle_types")
+
+    def initializeParticles(self, seed: int = 1, spawn_region: float = 2000.0) -> None:
+        check(self._lib.cf_initialize_particles(self._h, seed, spawn_region), "cf_initialize_particles")
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(self._lib.cf_set_stream(self._h, C.c_void_p(stream_ptr or 0)), "cf_set_stream")
+
+    def sync(self) -> None:
+        check(self._lib.cf_sync(self._h), "cf_sync")
+
+    # ---- state ----------------------------------------------------------------
+    def getParticleData(self) -> np.ndarray:
+        """AoS records in the reference layout (ParticleSimulation.cu:558-562)."""
+        n = self.getParticleCount()
+        out = np.zeros(n, dtype=PARTICLE_DTYPE)
+        check(self._lib.cf_get_particles(self._h, _ptr(out), n), "cf_get_particles")
+        return out
+
+    def setParticleData(self, records: np.ndarray) -> None:
+        rec = np.ascontiguousarray(records, dtype=PARTICLE_DTYPE)
+        check(self._lib.cf_set_particles(self._h, _ptr(rec), len(rec)), "cf_set_particles")
+
+    def set_particles(self, pos: np.ndarray, types: np.ndarray, vel: np.ndarray | None = None) -> None:
+        """Set positions (n, 3), types (n,) and optional velocities; counts reset to 0."""
+        n = self.getParticleCount()
+        pos4 = np.zeros((n, 4), dtype=np.float32)
+        pos4[:, :3] = pos
+        pos4[:, 3] = np.asarray(types, dtype=np.uint32).view(np.float32)
+        vel4 = np.zeros((n, 4), dtype=np.float32)
+        if vel is not None:
+            vel4[:, :3] = vel
+        counts = np.zeros(n, dtype=np.int32)
+        check(self._lib.cf_set_state(self._h, _ptr(pos4), _ptr(vel4), _ptr(counts)), "cf_set_state")
+
+    def get_state(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n = self.getParticleCount()
+        pos4 = np.zeros((n, 4), dtype=np.float32)
+        vel4 = np.zeros((n, 4), dtype=np.float32)
+        counts = np.zeros(n, dtype=np.int32)
+        check(self._lib.cf_get_state(self._h, _ptr(pos4), _ptr(vel4), _ptr(counts)), "cf_get_state")
+        return pos4, vel4, counts
+
+    def set_state(self, pos4: np.ndarray, vel4: np.ndarray, counts: np.ndarray) -> None:
+        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        vel4 = np.ascontiguousarray(vel4, dtype=np.float32)
+        counts = np.ascontiguousarray(counts, dtype=np.int32)
+        check(self._lib.cf_set_state(self._h, _ptr(pos4), _ptr(vel4), _ptr(counts)), "cf_set_state")
+
+    def getNeighborCounts(self) -> np.ndarray:
+        n = self.getParticleCount()
+        out = np.zeros(n, dtype=np.int32)
+        check(self._lib.cf_get_neighbor_counts(self._h, _ptr(out), n), "cf_get_neighbor_counts")
+        return out
+
+    def device_buffers(self) -> DeviceView:
+        v = DeviceView()
+        check(self._lib.cf_device_buffers(self._h, C.byref(v)), "cf_device_buffers")
+        return v
+
+    # ---- parameter surface ------------------------------------------------------
+    def getRawForceTableValues(self) -> np.ndarray:
+        t = self.getNumParticleTypes()
+        out = np.zeros(t * t, dtype=np.float32)
+        check(self._lib.cf_get_raw_force_table(self._h, _ptr(out), t * t), "cf_get_raw_force_table")
+        return out
+
+    def setRawForceTableValues(self, raw) -> None:
+        raw = np.ascontiguousarray(raw, dtype=np.float32).ravel()
+        check(self._lib.cf_set_raw_force_table(self._h, _ptr(raw), raw.size), "cf_set_raw_force_table")
+
+    def regenerateForceTable(self, seed: int = 1) -> None:
+        check(self._lib.cf_regenerate_force_table(self._h, seed), "cf_regenerate_force_table")
+
+    def updateForceTable(self, force_range: float, force_bias: float, force_offset: float) -> None:
+        check(self._lib.cf_update_force_table(self._h, force_range, force_bias, force_offset),
+              "cf_update_force_table")
+
+    def setForceTable(self, table) -> None:
+        table = np.ascontiguousarray(table, dtype=np.float32).ravel()
+        check(self._lib.cf_set_force_table(self._h, _ptr(table), table.size), "cf_set_force_table")
+
+    def getForceTable(self) -> np.ndarray:
+        t = self.getNumParticleTypes()
+        out = np.zeros(t * t, dtype=np.float32)
+        check(self._lib.cf_get_force_table(self._h, _ptr(out), t * t), "cf_get_force_table")
+        return out
+
+    def getRadioByType(self) -> np.ndarray:
+        t = self.getNumParticleTypes()
+        out = np.zeros(t, dtype=np.float32)
+        check(self._lib.cf_get_radio_by_type(self._h, _ptr(out), t), "cf_get_radio_by_type")
+        return out
+
+    def setRadioByType(self, values) -> None:
+        values = np.ascontiguousarray(values, dtype=np.float32).ravel()
+        check(self._lib.cf_set_radio_by_type(self._h, _ptr(values), values.size), "cf_set_radio_by_type")
+
+    def setRadioByTypeValue(self, index: int, value: float) -> None:
+        check(self._lib.cf_set_radio_by_type_value(self._h, index, value), "cf_set_radio_by_type_value")
+
+    def rotateRadioByType(self) -> None:
+        check(self._lib.cf_rotate_radio_by_type(self._h), "cf_rotate_radio_by_type")
+
+    # ---- step ---------------------------------------------------------------------
+    def simulate(self, params: SimulationParams, steps: int = 1) -> None:
+        """ParticleSimulation::simulate (ParticleSimulation.cu:541-556), `steps` times; asynchronous."""
+        p = params.to_c()
+        check(self._lib.cf_step(self._h, C.byref(p), steps), "cf_step")
+
+    def grid(self, params: SimulationParams) -> GridInfo:
+        g = GridInfo()
+        p = params.to_c()
+        check(self._lib.cf_get_grid(self._h, C.byref(p), C.byref(g)), "cf_get_grid")
+        return g
+
+    def cell_list(self, params: SimulationParams):
+        g = self.grid(params)
+        cells = g.cells[0] * g.cells[1] * g.cells[2]
+        n = self.getParticleCount()
+        cell_of = np.zeros(n, dtype=np.uint32)
+        order = np.zeros(n, dtype=np.uint32)
+        start = np.zeros(cells, dtype=np.uint32)
+        end = np.zeros(cells, dtype=np.uint32)
+        p = params.to_c()
+        check(self._lib.cf_debug_cell_list(self._h, C.byref(p), _ptr(cell_of), _ptr(order), _ptr(start),
+                                           _ptr(end), cells), "cf_debug_cell_list")
+        return g, cell_of, order, start, end
+
+    def work_counters(self, params: SimulationParams) -> tuple[int, int]:
+        c27 = C.c_uint64()
+        inter = C.c_uint64()
+        p = params.to_c()
+        check(self._lib.cf_work_counters(self._h, C.byref(p), C.byref(c27), C.byref(inter)), "cf_work_counters")
+        return c27.value, inter.value
+
+    # ---- proximity graph -----------------------------------------------------------
+    def proximity_edges(self, distance: float, max_conn: int, cap: int | None = None) -> np.ndarray:
+        """Edges (i, j) of generateProximityGraph (ParticleSimulation.cu:625-687), shape (E, 2)."""
+        if cap is None:
+            cap = self.getParticleCount() * max(max_conn, 0)
+        edges = np.zeros((max(cap, 1), 2), dtype=np.int32)
+        count = C.c_int()
+        check(self._lib.cf_proximity_edges(self._h, distance, max_conn, _ptr(edges), cap, C.byref(count)),
+              "cf_proximity_edges")
+        return edges[: count.value].copy()
+
+    def proximity_vertices_device(self, distance: float, max_conn: int, colors, vertices_ptr: int,
+                                  cap_vertices: int) -> int:
+        cols = (Color * len(colors))(*[Color(*c) for c in colors])
+        count = C.c_int()
+        check(self._lib.cf_proximity_vertices_device(self._h, distance, max_conn, cols, len(colors),
+                                                     C.c_void_p(vertices_ptr), cap_vertices, C.byref(count)),
+              "cf_proximity_vertices_device")
+        return count.value
+
+
+def lfo_ratio(ratio: float, lfo_a: float, lfo_s: float, t: float) -> float:
+    """Caller LFO of CellFlowWidget::paintGL (CellFlowWidget.cpp:414-421)."""
+    return load().cf_lfo_ratio(ratio, lfo_a, lfo_s, t)
+
+
+def version() -> str:
+    return load().cf_version().decode()
+
+
+__all__ = ["ParticleSimulation", "SimulationParams", "PARTICLE_DTYPE", "lfo_ratio", "version", "_lib"]

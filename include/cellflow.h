@@ -1,0 +1,238 @@
+/*
+ * cellflow.h - C ABI of the GB300 CellFlow simulation step.
+ *
+ * This ABI replaces the C++ class `ParticleSimulation`
+ * (cuda-native/include/ParticleSimulation.cuh:10-103) and the physics subset of
+ * `SimulationParams` (cuda-native/include/SimulationParams.h:14-37).  Every entry
+ * point below names the reference member it stands in for.
+ *
+ * Conventions
+ *   - Every function returns an int status: CF_OK (0) or a negative CF_ERR_*
+ *     code.  cf_last_error() returns a message for the last failure on the
+ *     calling thread.  The reference printed and called exit(1) instead
+ *     (cuda-native/src/ParticleSimulation.cu:10-18).
+ *   - One cf_world owns its device buffers and one CUDA stream.  Calls that
+ *     launch work are asynchronous on that stream; cf_sync() waits and reports
+ *     device-side errors (a particle that left the domain, a bounded wait that
+ *     gave up).  Calls that return data to host memory synchronise first.  A
+ *     handle is not re-entrant: use it from one thread at a time.
+ *   - Host pointers are plain host memory (pinned or pageable).  Functions with
+ *     a `_device` suffix take device pointers on the world's device.
+ *   - Positions live in the periodic box [0,W)x[0,H)x[0,D).  The step keeps the
+ *     reference's Jacobi-consistent meaning: every particle sees the positions
+ *     of the start of the step (the reference kernel raced here, reading slots
+ *     other threads were rewriting; ParticleSimulation.cu:89 vs :164).
+ */
+#ifndef CELLFLOW_H
+#define CELLFLOW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CF_OK 0
+#define CF_ERR_INVALID (-1)  /* bad argument or size                        */
+#define CF_ERR_CUDA (-2)     /* a CUDA runtime call failed                    */
+#define CF_ERR_ALLOC (-3)    /* device or host allocation failed              */
+#define CF_ERR_DOMAIN (-4)   /* a position is outside [0,W) or not finite     */
+#define CF_ERR_DEVICE (-5)   /* a kernel raised its error word                */
+#define CF_ERR_CAPACITY (-6) /* an output buffer is too small                 */
+
+#define CF_MAX_TYPES 32     /* the reference capped at 10 (SimulationParams.h:64) */
+#define CF_MAX_PROX_CONN 16 /* the reference overflowed nearby[32] above 16 (ParticleSimulation.cu:210,215) */
+
+/* Particle record, byte-compatible with the reference `Particle`
+ * (SimulationParams.h:6-12): 44 bytes, pos, vel, acc, type, pad. */
+typedef struct cf_particle {
+    float pos[3];
+    float vel[3];
+    float acc[3];
+    uint32_t ptype;
+    float pad;
+} cf_particle;
+
+/* RGB colour per type, the reference `ParticleColor` (SimulationParams.h:60-62). */
+typedef struct cf_color {
+    float r, g, b;
+} cf_color;
+
+/* Physics parameters of one step: the fields of `SimulationParams`
+ * (SimulationParams.h:15-29) that the step kernel reads
+ * (ParticleSimulation.cu:97-161), in the same order and meaning. */
+typedef struct cf_step_params {
+    float radius;               /* interaction radius                         */
+    float delta_t;              /* time step                                  */
+    float friction;             /* velocity multiplier per step               */
+    float repulsion;            /* repulsion amplitude                        */
+    float attraction;           /* attraction slope                           */
+    float k;                    /* repulsion decay                            */
+    float balance;              /* density balance                            */
+    float canvas_width;         /* W: box extent in x                         */
+    float canvas_height;        /* H: box extent in y                         */
+    float canvas_depth;         /* D: box extent in z                         */
+    int num_particle_types;     /* T                                          */
+    float ratio_with_lfo;       /* per-type radius modulation ratio           */
+    float force_multiplier;     /* global force scale                         */
+    int max_expected_neighbors; /* density normaliser                         */
+} cf_step_params;
+
+typedef struct cf_world cf_world;
+
+/* Grid chosen for a step (introspection for tests and tools). */
+typedef struct cf_grid_info {
+    int cells[3];      /* cells per axis                                      */
+    float inv_cell[3]; /* cells per unit length, the hash multiplier          */
+    float r_max;       /* largest effective radius over type pairs            */
+    int generic_wrap;  /* 1: per-candidate reference wrap; 0: per-cell shift  */
+    int key_bits;      /* bits of the linear cell id                          */
+} cf_grid_info;
+
+/* Device buffers of a world (all in original particle order). */
+typedef struct cf_device_view {
+    void* pos4;   /* float4[n]: x, y, z, type (uint32 bits in .w)             */
+    void* vel4;   /* float4[n]: vx, vy, vz, 0                                 */
+    void* acc4;   /* float4[n]: ax, ay, az, 0 (the last step's scaled force)  */
+    void* counts; /* int32[n]: neighbour counts of the last step              */
+    int n;
+} cf_device_view;
+
+/* ---- library ----------------------------------------------------------- */
+
+const char* cf_last_error(void);
+const char* cf_version(void);
+/* SimulationParams defaults (SimulationParams.h:15-29). */
+void cf_default_params(cf_step_params* p);
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* ParticleSimulation(int) / (int, float, float) (ParticleSimulation.cuh:12-13,
+ * ParticleSimulation.cu:427-445).  Allocates n particles of num_types types in
+ * a W x H x D box, fills a seeded force table and radius table and spawns the
+ * particles with cf_initialize_particles(seed, min(2000, box)). */
+int cf_create(int n, int num_types, float w, float h, float d, uint64_t seed, cf_world** out);
+/* ~ParticleSimulation (ParticleSimulation.cu:447-449). */
+int cf_destroy(cf_world* w);
+/* Run the world's work on a caller-owned cudaStream_t (NULL restores the
+ * world's own stream).  The caller keeps the stream alive. */
+int cf_set_stream(cf_world* w, void* cuda_stream);
+int cf_sync(cf_world* w);
+int cf_particle_count(const cf_world* w, int* n);
+int cf_num_particle_types(const cf_world* w, int* t);
+
+/* setParticleCount (ParticleSimulation.cu:564-572): reallocates and respawns. */
+int cf_set_particle_count(cf_world* w, int n, uint64_t seed);
+/* setNumParticleTypes (ParticleSimulation.cu:574-579): new type count, new
+ * seeded raw table and radius table, respawn. */
+int cf_set_num_particle_types(cf_world* w, int t, uint64_t seed);
+/* initializeParticles (ParticleSimulation.cu:484-505, kernel :29-66): uniform
+ * positions in a centred spawn cube of side min(spawn, extent), zero velocity
+ * and acceleration, uniform types.  Seeded counter-based generator instead of
+ * the reference's time-seeded cuRAND state; the type is clamped to T-1 (the
+ * reference could produce T when its uniform draw was exactly 1.0). */
+int cf_initialize_particles(cf_world* w, uint64_t seed, float spawn_region);
+
+/* ---- particle state ---------------------------------------------------- */
+
+/* getParticleData (ParticleSimulation.cu:558-562): AoS 44-byte records. */
+int cf_get_particles(cf_world* w, cf_particle* out, int n);
+/* Upload AoS records (the reference had no setter; its init kernel wrote
+ * them).  Positions must lie in [0,W)x[0,H)x[0,D), types in [0,T). */
+int cf_set_particles(cf_world* w, const cf_particle* in, int n);
+/* Structure-of-arrays state: pos4/vel4 are float[4n] (type bits in pos4.w),
+ * counts int[n] (the neighbour counts the next step reads as "previous"). */
+int cf_get_state(cf_world* w, float* pos4, float* vel4, int* counts);
+int cf_set_state(cf_world* w, const float* pos4, const float* vel4, const int* counts);
+/* The neighbour counts written by the last step (neighborCountsOut,
+ * ParticleSimulation.cu:165). */
+int cf_get_neighbor_counts(cf_world* w, int* out, int n);
+int cf_device_buffers(cf_world* w, cf_device_view* out);
+
+/* ---- parameter surface ------------------------------------------------- */
+
+/* getRawForceTableValues (ParticleSimulation.cuh:47): T*T raw values. */
+int cf_get_raw_force_table(cf_world* w, float* raw, int count);
+int cf_set_raw_force_table(cf_world* w, const float* raw, int count);
+/* regenerateForceTable / initializeForceTable (ParticleSimulation.cu:513-519,
+ * 581-583): raw values uniform in [-1,1] from a seeded generator, then
+ * updateForceTable(0.28, -0.20, 1.0). */
+int cf_regenerate_force_table(cf_world* w, uint64_t seed);
+/* updateForceTable (ParticleSimulation.cu:521-531):
+ * F = clamp(tanhf(raw*offset)*range + bias, -1, 1), row-major [self*T+other]. */
+int cf_update_force_table(cf_world* w, float range, float bias, float offset);
+/* Set the final device table directly (T*T values, used unclamped). */
+int cf_set_force_table(cf_world* w, const float* table, int count);
+int cf_get_force_table(cf_world* w, float* table, int count);
+/* radioByType (ParticleSimulation.cu:533-539, 594-622). */
+int cf_get_radio_by_type(cf_world* w, float* out, int count);
+int cf_set_radio_by_type(cf_world* w, const float* values, int count);
+int cf_set_radio_by_type_value(cf_world* w, int index, float value);
+int cf_rotate_radio_by_type(cf_world* w);
+/* The caller-side LFO of CellFlowWidget::paintGL (CellFlowWidget.cpp:414-421):
+ * returns ratio + lfo_a*sin(2*pi*lfo_s*t), or ratio when lfo_a == 0. */
+float cf_lfo_ratio(float ratio, float lfo_a, float lfo_s, float t_seconds);
+
+/* ---- the step ----------------------------------------------------------- */
+
+/* simulate (ParticleSimulation.cu:541-556), run nsteps times.  Each step
+ * builds the cell list, computes forces, neighbour counts and the
+ * density-adaptive scale, integrates and wraps.  Asynchronous. */
+int cf_step(cf_world* w, const cf_step_params* p, int nsteps);
+/* The grid cf_step would use for these parameters. */
+int cf_get_grid(cf_world* w, const cf_step_params* p, cf_grid_info* out);
+/* Build the cell list of the current positions with the step's grid and
+ * return it: cell id per particle, particle indices in stable cell order,
+ * and per-cell [start,end) into that order (cells with no particle: 0,0).
+ * Sizes: n, n, cells, cells where cells = product of cf_grid_info.cells. */
+int cf_debug_cell_list(cf_world* w, const cf_step_params* p, uint32_t* cell_of, uint32_t* sorted_idx,
+                       uint32_t* cell_start, uint32_t* cell_end, int cells_cap);
+/* Work counters of the current positions with the canonical grid of the
+ * work model (cells per axis floor(L/r_max)): directed candidate pairs in
+ * the 27-cell stencil (C27) and directed interacting pairs (I). */
+int cf_work_counters(cf_world* w, const cf_step_params* p, uint64_t* c27, uint64_t* interacting);
+
+/* ---- proximity graph ---------------------------------------------------- */
+
+/* generateProximityGraph (ParticleSimulation.cu:625-687, kernel :188-277) with
+ * the GL buffer replaced by plain output.  For each particle i: the first
+ * 2*max_conn particles j>i of the same type with non-periodic squared distance
+ * below distance^2, in index order; of those the max_conn nearest (ties keep
+ * index order).  Edges are written as (i, j) pairs, ordered by i, then by
+ * distance.  max_conn must be in [0, CF_MAX_PROX_CONN].  Writes up to cap
+ * edges to `edges` (int32[2*cap], host); *n_edges receives the full count
+ * (CF_ERR_CAPACITY when it exceeds cap). */
+int cf_proximity_edges(cf_world* w, float distance, int max_conn, int32_t* edges, int cap, int* n_edges);
+/* Same edge set, written as the reference's line vertices: per edge two
+ * vertices of 6 floats (x, y, z, r, g, b), colour of particle i's type
+ * (colors[type % T]).  `vertices` is a DEVICE buffer of cap_vertices*6
+ * floats standing in for the GL VBO; *vertex_count = 2 * edges. */
+int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, const cf_color* colors, int n_colors,
+                                 float* vertices, int cap_vertices, int* vertex_count);
+
+/* ---- measurement ---------------------------------------------------------- */
+
+/* Device time of the step's phases, accumulated over the steps run since
+ * profiling was enabled or last read, from CUDA events recorded on the
+ * world's stream around each phase. */
+typedef struct cf_phase_times {
+    double cell_list_ms; /* hash + radix sort + start/end + sorted snapshot */
+    double force_ms;     /* force + density + integrator kernel           */
+    long long steps;     /* steps covered                                  */
+    long long launches;  /* kernel launches of the library in those steps  */
+} cf_phase_times;
+
+/* No counterpart in the reference (it had only a frame counter,
+ * CellFlowWidget.cpp:705-713).  Enabling adds two events per phase. */
+int cf_profile_enable(cf_world* w, int on);
+int cf_profile_read(cf_world* w, cf_phase_times* out);
+/* Measured FP32 FMA throughput of the current device in TFLOP/s (an FMA
+ * counts 2 flops): dependent FMA chains on every SM, timed with events. */
+int cf_measure_fp32_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CELLFLOW_H */
