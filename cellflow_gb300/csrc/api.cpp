@@ -269,17 +269,18 @@ int prepare_step(cf_world* w, const cf_step_params* p, StepConsts* c)
 }
 
 // One step's launches on the world's stream: cell list, then the fused force,
-// density and integrator kernel; with the three profiling events when prof.
+// density and integrator kernel; with the three profiling events when prof
+// (recorded as external event nodes when the stream is being captured).
 int enqueue_step(cf_world* w, const StepConsts& c, int prof)
 {
-    if (prof) CF_CUDA(cudaEventRecord(w->prof_ev[0], w->stream));
+    if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[0], w->stream, cudaEventRecordExternal));
     int which = 0;
     int rc = build_cell_list(w, c.grid, c.ext, &which);
     if (rc) return rc;
-    if (prof) CF_CUDA(cudaEventRecord(w->prof_ev[1], w->stream));
+    if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[1], w->stream, cudaEventRecordExternal));
     CF_CUDA(launch_step_force(c, w->tables, w->s.pos_sorted, w->s.keys[which], w->s.vals[which], w->s.cell_start,
                               w->s.cell_end, w->pos, w->vel, w->acc, w->counts, w->stream));
-    if (prof) CF_CUDA(cudaEventRecord(w->prof_ev[2], w->stream));
+    if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[2], w->stream, cudaEventRecordExternal));
     return CF_OK;
 }
 
