@@ -150,6 +150,11 @@ _SIGNATURES = {
         C.c_int,
         [_W, C.c_float, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, _P(C.c_int)],
     ),
+    "cf_proximity_edges_noalloc": (
+        C.c_int,
+        [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p, C.c_int,
+         _P(C.c_int), C.c_void_p],
+    ),
     "cf_profile_enable": (C.c_int, [_W, C.c_int]),
     "cf_profile_read": (C.c_int, [_W, _P(PhaseTimes)]),
     "cf_measure_fp32_peak": (C.c_int, [_P(C.c_double)]),

@@ -211,6 +211,30 @@ int cf_proximity_edges(cf_world* w, float distance, int max_conn, int32_t* edges
 int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, const cf_color* colors, int n_colors,
                                  float* vertices, int cap_vertices, int* vertex_count);
 
+/* Proximity edges without allocating: the same edges, in the same order, as
+ * cf_proximity_edges, for callers that may not allocate device memory while
+ * they run -- a renderer's frame loop building the graph every frame (an
+ * allocation can stall the device inside the frame), or a host application
+ * whose device memory is owned by its own pool.  No counterpart in the
+ * reference (its wrapper allocated and freed buffers on every call).
+ *   d_pos4   DEVICE float4[n]: x, y, z, type bits (cf_device_view.pos4 layout),
+ *            positions inside [0,width)x[0,height)x[0,depth)
+ *   d_edges  DEVICE int32[2*cap] receiving (i, j) pairs; *n_edges (host) the
+ *            full count (CF_ERR_CAPACITY when it exceeds cap)
+ *   stream   cudaStream_t the work runs on (NULL: the legacy default stream);
+ *            the call waits for it before returning
+ * Limits: n <= 65536 (CF_ERR_INVALID above); the proximity grid is coarsened
+ * to at most 65536 cells.  All scratch lives in one fixed device array of
+ * about 6.9 MB that every device holds from the library's first use there
+ * until the process exits.  The first call on a device looks up that array's
+ * address, so make it before any stream capture.  Calls share the array and
+ * it keeps the previous call's contents (the call clears what must start at
+ * zero): calls whose work overlaps on the GPU -- other streams, other threads
+ * on the same device -- race and must be serialised by the caller.
+ * It calls no cudaMalloc, cudaFree or other allocating routine. */
+int cf_proximity_edges_noalloc(const void* d_pos4, int n, float width, float height, float depth, float distance,
+                               int max_conn, int32_t* d_edges, int cap, int* n_edges, void* stream);
+
 /* ---- measurement ---------------------------------------------------------- */
 
 /* Device time of the step's phases, accumulated over the steps run since
