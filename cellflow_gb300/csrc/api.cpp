@@ -115,6 +115,10 @@ void free_particles(cf_world* w)
     dev_free(s.prox_count);
     dev_free(s.counters);
     dev_free(s.cell_pop);
+    dev_free(s.row_count);
+    dev_free(s.items);
+    dev_free(s.n_items);
+    dev_free(s.cell_off);
     dev_free(w->aos);
     w->pos = w->vel = w->acc = nullptr;
     w->counts = nullptr;
@@ -135,6 +139,56 @@ int ensure_cells(cf_world* w, int cells)
     CF_CUDA(dev_alloc(&s.cell_start, cells));
     CF_CUDA(dev_alloc(&s.cell_end, cells));
     s.cells_cap = (size_t)cells;
+    return CF_OK;
+}
+
+// CSR offsets (cells + 1 entries) and the scan partials they need.
+int ensure_offsets(cf_world* w, int cells)
+{
+    Scratch& s = w->s;
+    const size_t need_tmp = scan_tmp_entries(cells + 1);
+    if ((size_t)cells + 1 <= s.off_cap && need_tmp <= s.scan_tmp_cap) return CF_OK;
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    drop_graphs(w);
+    if ((size_t)cells + 1 > s.off_cap) {
+        dev_free(s.cell_off);
+        s.cell_off = nullptr;
+        s.off_cap = 0;
+        CF_CUDA(dev_alloc(&s.cell_off, (size_t)cells + 1));
+        s.off_cap = (size_t)cells + 1;
+    }
+    if (need_tmp > s.scan_tmp_cap) {
+        dev_free(s.scan_tmp);
+        s.scan_tmp = nullptr;
+        s.scan_tmp_cap = 0;
+        CF_CUDA(dev_alloc(&s.scan_tmp, need_tmp));
+        s.scan_tmp_cap = need_tmp;
+    }
+    return CF_OK;
+}
+
+// Buffers of the force kernel's plan for this grid: per-row populations and
+// the item list (at most n/32 + rows items).
+int ensure_plan(cf_world* w, const Grid& g)
+{
+    Scratch& s = w->s;
+    const size_t rows = (size_t)g.m[1] * g.m[2];
+    const size_t items = (size_t)max_step_items(w->n, g);
+    if (rows <= s.rows_cap && items <= s.items_cap && s.n_items) return CF_OK;
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    drop_graphs(w);
+    dev_free(s.row_count);
+    dev_free(s.items);
+    dev_free(s.n_items);
+    s.row_count = nullptr;
+    s.items = nullptr;
+    s.n_items = nullptr;
+    s.rows_cap = s.items_cap = 0;
+    CF_CUDA(dev_alloc(&s.row_count, rows));
+    CF_CUDA(dev_alloc(&s.items, items));
+    CF_CUDA(dev_alloc(&s.n_items, 1));
+    s.rows_cap = rows;
+    s.items_cap = items;
     return CF_OK;
 }
 
@@ -174,7 +228,7 @@ int sync_and_check(cf_world* w)
 // radius per type pair in the reference's float expression, the exact
 // sqrt threshold, and the force table; uploaded when anything changed.
 int update_pair_tables(cf_world* w, const cf_step_params* p, float* r_cut, int* uniform_r, float* eff_u,
-                       float* thr_u)
+                       float* thr_u, float* thr_max_out)
 {
     const int T = w->num_types;
     PairTables& h = w->host_tables;
@@ -211,6 +265,7 @@ int update_pair_tables(cf_world* w, const cf_step_params* p, float* r_cut, int* 
             uniform = uniform && eff_bits[k] == eff_bits[0];
         }
     *r_cut = cutoff_distance(thr_max);
+    *thr_max_out = thr_max;
     *uniform_r = uniform ? 1 : 0;
     *eff_u = h.eff[0];
     *thr_u = h.threshold[0];
@@ -242,18 +297,36 @@ int build_cell_list(cf_world* w, const Grid& g, const float* ext, int* which)
     return CF_OK;
 }
 
+// Bound for the force kernel's approximate pre-test: every pair whose exact
+// test fl(d^2 + 1e-4) < t passes fl(fma-contracted d^2 of a pre-shifted
+// displacement) < bound.  The displacements differ by at most delta per axis
+// (two roundings at the box scale); the rest is relative rounding slack.
+float filter_bound(float thr_max, float max_extent)
+{
+    if (std::isinf(thr_max)) return INFINITY;
+    const double b = ((double)thr_max * (1.0 + 0x1p-24) - (double)0.0001f) / (1.0 - 0x1p-22);
+    if (!(b > 0.0)) return -1.0f;
+    int ex = 0;
+    std::frexp(2.0 * (double)max_extent, &ex);
+    const double delta = 2.0 * std::ldexp(1.0, ex - 24);  // 2 ulp of 2 * extent
+    const double bound = (b + 3.47 * delta * std::sqrt(b) + 3.0 * delta * delta) * (1.0 + 0x1p-21);
+    return nextafterf((float)bound, INFINITY);
+}
+
 int prepare_step(cf_world* w, const cf_step_params* p, StepConsts* c)
 {
     int rc = check_params(w, p);
     if (rc) return rc;
-    float r_cut = 0.0f;
+    float r_cut = 0.0f, thr_max = 0.0f;
     std::memset(c, 0, sizeof(*c));
-    rc = update_pair_tables(w, p, &r_cut, &c->uniform_r, &c->eff_uniform, &c->thr_uniform);
+    rc = update_pair_tables(w, p, &r_cut, &c->uniform_r, &c->eff_uniform, &c->thr_uniform, &thr_max);
     if (rc) return rc;
     c->ext[0] = p->canvas_width;
     c->ext[1] = p->canvas_height;
     c->ext[2] = p->canvas_depth;
     for (int a = 0; a < 3; a++) c->half[a] = c->ext[a] * 0.5f;
+    c->inv_eff_uniform = 1.0f / c->eff_uniform;
+    c->thr_filter = filter_bound(thr_max, std::max(c->ext[0], std::max(c->ext[1], c->ext[2])));
     c->grid = choose_step_grid(c->ext, r_cut, kMaxCells);
     c->n = w->n;
     c->num_types = w->num_types;
@@ -275,11 +348,14 @@ int enqueue_step(cf_world* w, const StepConsts& c, int prof)
 {
     if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[0], w->stream, cudaEventRecordExternal));
     int which = 0;
-    int rc = build_cell_list(w, c.grid, c.ext, &which);
-    if (rc) return rc;
+    Scratch& s = w->s;
+    CF_CUDA(launch_cell_list_csr(w->pos, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, w->err, &which,
+                                 w->stream));
+    CF_CUDA(launch_step_plan(s.cell_off, w->n, c.grid, s.items, s.n_items, w->stream));
     if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[1], w->stream, cudaEventRecordExternal));
-    CF_CUDA(launch_step_force(c, w->tables, w->s.pos_sorted, w->s.keys[which], w->s.vals[which], w->s.cell_start,
-                              w->s.cell_end, w->pos, w->vel, w->acc, w->counts, w->stream));
+    CF_CUDA(launch_step_force(c, w->tables, s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.items,
+                              s.n_items, max_step_items(w->n, c.grid), w->pos, w->vel, w->acc, w->counts,
+                              w->stream));
     if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[2], w->stream, cudaEventRecordExternal));
     return CF_OK;
 }
@@ -827,13 +903,17 @@ int cf_step(cf_world* w, const cf_step_params* p, int nsteps)
     if (rc) return rc;
     rc = ensure_cells(w, c.grid.cells);
     if (rc) return rc;
+    rc = ensure_plan(w, c.grid);
+    if (rc) return rc;
+    rc = ensure_offsets(w, c.grid.cells);
+    if (rc) return rc;
     const int prof = w->profiling ? 1 : 0;
     cudaGraphExec_t exec = nullptr;
     if (w->use_graphs && w->stream != nullptr && nsteps > 0) {
         rc = step_graph(w, c, prof, &exec);
         if (rc) return rc;
     }
-    const long long launches = cell_list_launches(w->n, c.grid.key_bits) + (w->n > 0 ? 1 : 0);
+    const long long launches = cell_list_csr_launches(w->n, c.grid.key_bits, c.grid.cells) + step_launches(w->n);
     for (int s = 0; s < nsteps; s++) {
         if (exec)
             CF_CUDA(cudaGraphLaunch(exec, w->stream));
@@ -914,9 +994,14 @@ int cf_debug_cell_list(cf_world* w, const cf_step_params* p, uint32_t* cell_of, 
     rc = prepare_step(w, p, &c);
     if (rc) return rc;
     if (cells_cap < c.grid.cells) return fail(CF_ERR_CAPACITY, "cell arrays smaller than the grid");
-    int which = 0;
-    rc = build_cell_list(w, c.grid, c.ext, &which);
+    rc = ensure_cells(w, c.grid.cells);
     if (rc) return rc;
+    rc = ensure_offsets(w, c.grid.cells);
+    if (rc) return rc;
+    // the step's own cell list: CSR offsets, stable radix order
+    int which = 0;
+    CF_CUDA(launch_cell_list_csr(w->pos, w->n, c.grid, c.ext, w->num_types, w->s, w->s.cell_off, w->err, &which,
+                                 w->stream));
     // the hash wrote cell ids in original order into keys[0] before sorting;
     // recompute them (the sort may have reused that buffer)
     CF_CUDA(launch_cell_hash(w->pos, w->n, c.grid, c.ext, w->num_types, w->s.keys[which ^ 1], w->err, w->stream));
@@ -926,13 +1011,16 @@ int cf_debug_cell_list(cf_world* w, const cf_step_params* p, uint32_t* cell_of, 
         if (sorted_idx)
             CF_CUDA(cudaMemcpyAsync(sorted_idx, w->s.vals[which], 4 * n, cudaMemcpyDeviceToHost, w->stream));
     }
-    if (cell_start)
-        CF_CUDA(cudaMemcpyAsync(cell_start, w->s.cell_start, 4 * (size_t)c.grid.cells, cudaMemcpyDeviceToHost,
-                                w->stream));
-    if (cell_end)
-        CF_CUDA(
-            cudaMemcpyAsync(cell_end, w->s.cell_end, 4 * (size_t)c.grid.cells, cudaMemcpyDeviceToHost, w->stream));
-    return sync_and_check(w);
+    std::vector<uint32_t> off((size_t)c.grid.cells + 1);
+    CF_CUDA(cudaMemcpyAsync(off.data(), w->s.cell_off, 4 * off.size(), cudaMemcpyDeviceToHost, w->stream));
+    rc = sync_and_check(w);
+    if (rc) return rc;
+    for (int k = 0; k < c.grid.cells; k++) {
+        const bool empty = off[k + 1] == off[k];
+        if (cell_start) cell_start[k] = empty ? 0u : off[k];
+        if (cell_end) cell_end[k] = empty ? 0u : off[k + 1];
+    }
+    return CF_OK;
 }
 
 int cf_work_counters(cf_world* w, const cf_step_params* p, uint64_t* c27, uint64_t* interacting)

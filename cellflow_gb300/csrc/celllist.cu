@@ -42,6 +42,35 @@ __global__ void __launch_bounds__(kThreads)
     keys[i] = (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
 }
 
+// Cell id of every particle and the population of every cell (counts must be
+// zero on entry); flags positions and types like cell_hash_kernel.
+__global__ void __launch_bounds__(kThreads)
+    cell_hash_count_kernel(const float4* __restrict__ pos, int n, Grid g, float ex, float ey, float ez, int num_types,
+                           uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, int* __restrict__ err)
+{
+    int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos[i];
+    bool inside = (p.x >= 0.0f && p.x < ex) && (p.y >= 0.0f && p.y < ey) && (p.z >= 0.0f && p.z < ez);
+    if (!inside) atomicOr(err, kDevErrDomain);
+    if (__float_as_uint(p.w) >= (uint32_t)num_types) atomicOr(err, kDevErrType);
+    int cx = cell_coord(p.x, g.inv[0], g.m[0]);
+    int cy = cell_coord(p.y, g.inv[1], g.m[1]);
+    int cz = cell_coord(p.z, g.inv[2], g.m[2]);
+    const uint32_t key = (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
+    keys[i] = key;
+    atomicAdd(&counts[key], 1u);
+}
+
+// The position snapshot in sorted (cell) order.
+__global__ void __launch_bounds__(kThreads)
+    gather_sorted_kernel(const uint32_t* __restrict__ vals, int n, const float4* __restrict__ pos,
+                         float4* __restrict__ pos_sorted)
+{
+    int t = blockIdx.x * kThreads + threadIdx.x;
+    if (t < n) pos_sorted[t] = pos[vals[t]];
+}
+
 // Digit histogram of one tile of kThreads*ITEMS keys, written digit-major:
 // hist[digit * nblocks + block].
 template <int ITEMS>
@@ -376,6 +405,43 @@ cudaError_t launch_cell_bounds(const uint32_t* keys, const uint32_t* vals, int n
     if (n <= 0) return cudaSuccess;
     cell_bounds_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(keys, vals, n, pos, start, end, pos_sorted);
     return cudaGetLastError();
+}
+
+// Cell list in CSR form for the step: keys[0] = cell ids, radix-sorted
+// (keys, vals)[*which], cell_off[c] = particles in cells < c (cells + 1
+// entries), pos_sorted = positions in sorted order.
+cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
+                                 Scratch& s, uint32_t* cell_off, int* err, int* which, cudaStream_t st)
+{
+    *which = 0;
+    cudaError_t e = cudaMemsetAsync(cell_off, 0, sizeof(uint32_t) * ((size_t)g.cells + 1), st);
+    if (e != cudaSuccess) return e;
+    if (n > 0) {
+        cell_hash_count_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(pos, n, g, ext[0], ext[1], ext[2],
+                                                                            num_types, s.keys[0], cell_off, err);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    e = launch_radix_sort(s, n, g.key_bits, which, st);
+    if (e != cudaSuccess) return e;
+    e = launch_scan_exclusive(cell_off, cell_off, g.cells + 1, s.scan_tmp, s.scan_tmp_cap, st);
+    if (e != cudaSuccess) return e;
+    if (n > 0) {
+        gather_sorted_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.vals[*which], n, pos, s.pos_sorted);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+int cell_list_csr_launches(int n, int key_bits, int cells)
+{
+    if (n <= 0) return 0;
+    int passes = (key_bits + 7) / 8;
+    if (passes < 1) passes = 1;
+    int entries = (int)radix_hist_entries(n);
+    int scan = blocks_for(entries, kScanTile) == 1 ? 1 : 3;
+    int cscan = blocks_for(cells + 1, kScanTile) == 1 ? 1 : 3;
+    return 1 + passes * (2 + scan) + cscan + 1;
 }
 
 cudaError_t launch_work_counters(const float4* pos, const int* counts, int n, const Grid& canon, uint32_t* pop,

@@ -60,6 +60,8 @@ struct StepConsts {
     int uniform_r;     // all pairs share one effective radius
     float eff_uniform;
     float thr_uniform;
+    float inv_eff_uniform;
+    float thr_filter;  // squared-distance bound of the approximate pre-test (>= every exact pass)
     float repulsion, attraction, neg_k, balance, force_multiplier, delta_t, friction;
     int max_expected_neighbors;
 };
@@ -83,6 +85,15 @@ struct Scratch {
     unsigned long long* counters = nullptr;  // [0] C27, [1] I
     uint32_t* cell_pop = nullptr;            // canonical-grid populations
     size_t pop_cap = 0;
+    // CSR cell offsets of the step (cells + 1 entries)
+    uint32_t* cell_off = nullptr;
+    size_t off_cap = 0;
+    // force-kernel plan: per-row populations and the row-aligned 32-particle items
+    uint32_t* row_count = nullptr;
+    size_t rows_cap = 0;
+    int2* items = nullptr;       // (first sorted index, particles) per item
+    size_t items_cap = 0;
+    int* n_items = nullptr;
 };
 
 }  // namespace cf
@@ -144,14 +155,22 @@ cudaError_t launch_radix_sort(Scratch& s, int n, int key_bits, int* which, cudaS
 cudaError_t launch_cell_bounds(const uint32_t* keys, const uint32_t* vals, int n, const float4* pos, uint32_t* start,
                                uint32_t* end, int cells, float4* pos_sorted, cudaStream_t st);
 cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
-                              const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_start,
-                              const uint32_t* cell_end, float4* pos, float4* vel, float4* acc, int* counts,
-                              cudaStream_t st);
+                              const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
+                              const int2* items, const int* n_items, int max_items, float4* pos, float4* vel,
+                              float4* acc, int* counts, cudaStream_t st);
+// Row-aligned items of at most 32 sorted particles (one cell row each).
+cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, int2* items, int* n_items,
+                             cudaStream_t st);
+int max_step_items(int n, const Grid& g);
+int step_launches(int n);
 cudaError_t launch_scan_exclusive(const uint32_t* in, uint32_t* out, int n, uint32_t* tmp, size_t tmp_cap,
                                   cudaStream_t st);
 size_t scan_tmp_entries(int n);
 size_t radix_hist_entries(int n);
 int cell_list_launches(int n, int key_bits);
+cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
+                                 Scratch& s, uint32_t* cell_off, int* err, int* which, cudaStream_t st);
+int cell_list_csr_launches(int n, int key_bits, int cells);
 cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* keys_sorted,
                                     const uint32_t* vals_sorted, const uint32_t* cell_start,
                                     const uint32_t* cell_end, const Grid& g, int n, float dsq, int max_conn,

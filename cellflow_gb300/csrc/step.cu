@@ -1,23 +1,38 @@
 // step.cu - pairwise smooth force, neighbour density and friction integrator.
 //
-// One thread per particle in cell order (the sorted snapshot of positions),
-// fused with the integrator; results are written back to original order.
+// Work decomposition.  Particles are in cell order (the sorted snapshot of
+// positions).  An item is up to 32 consecutive particles of one row of cells
+// (same y and z cell): one warp, one particle per lane.  The candidates of
+// an item are the particles of the union of its homes' 27-cell stencils:
+// 9 rows, each a run of consecutive cells, i.e. one contiguous range of the
+// sorted snapshot (two where the run wraps around the box in x).  The warp
+// copies those ranges into shared memory with coalesced loads, 256 at a
+// time, and every lane tests every staged candidate (broadcast reads).
 //
-// Arithmetic follows cuda-native/src/ParticleSimulation.cu:86-165 operation
-// by operation with round-to-nearest intrinsics, which nvcc never contracts:
-//   - the neighbour test is exact: d^2 = (dx*dx + dy*dy) + dz*dz and
+// Per batch of staged candidates, two phases per lane:
+//   Filter: squared distances of two candidates per instruction (packed f32x2
+//     add/mul/fma of sm_100+) from the lane's home to candidates staged with
+//     their segment's periodic shift already applied, against a bound that
+//     is >= the exact test for every pair.  The result is one 32-bit mask per
+//     32 candidates; about 85% of pairs fail here.
+//   Drain: for every set bit, the reference's exact test on the unshifted
+//     coordinates and, when it passes, the force term.
+//
+// Exactness (cuda-native/src/ParticleSimulation.cu:86-165):
+//   - the neighbour test is the reference's: d^2 = (dx*dx + dy*dy) + dz*dz and
 //     s = d^2 + 1e-4 rounded as the reference (compiled without contraction)
 //     rounds them, and sqrtf(s) < eff is replaced by the equivalent s < t,
-//     t the smallest float whose correctly rounded square root is >= eff, so
+//     t the smallest float whose correctly rounded square root is >= eff;
 //     neighbour counts match bit for bit;
-//   - the periodic wrap of a displacement is the reference's subtraction of
-//     the extent, applied where the reference's test would fire: with at
-//     least 5 cells on every axis that is exactly the stencil cells across
-//     the box edge, so it is one add of a per-cell shift; with fewer cells
-//     the kernel runs the reference's two tests per candidate;
-//   - force terms use correctly rounded sqrt and division as the reference
-//     does; only expf differs (CUDA's, within 2 ulp) and the summation order
-//     (cell order instead of index order).
+//   - a displacement is wrapped like the reference (subtract the extent where
+//     its test fires).  With at least 5 cells per axis that is exactly the
+//     stencil cells across the box edge: the union of an item spans at most
+//     the box width in x, so every staged range has one shift for every
+//     lane, added after the subtraction as the reference does.  With fewer
+//     cells both phases run the reference's tests per candidate;
+//   - force terms use rsqrt and exp approximations (a few ulp) instead of the
+//     reference's sqrtf, divisions and expf; the sum runs in cell order.
+//   The density factor, integrator and wrap are the reference's operations.
 #include <cuda_runtime.h>
 
 #include "cf_internal.hpp"
@@ -25,7 +40,11 @@
 namespace cf {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kWarps = 4;
+constexpr int kThreads = 32 * kWarps;
+constexpr int kStage = 256;  // staged candidates per batch (multiple of 32)
+constexpr int kGroups = kStage / 32;
+constexpr float kFar = 1e30f;  // padding slots sit at +kFar, idle homes at -kFar
 
 __device__ __forceinline__ float wrap_ref(float d, float ext, float half)
 {
@@ -35,151 +54,357 @@ __device__ __forceinline__ float wrap_ref(float d, float ext, float half)
     return d;
 }
 
+// Shift code per axis: 0 none, 1 subtract the extent, 2 add it.
+__device__ __forceinline__ float code_shift(uint32_t code, float ext)
+{
+    return code == 1u ? -ext : (code == 2u ? ext : 0.0f);
+}
+
+__device__ __forceinline__ int wrap_index(int v, int m) { return v < 0 ? v + m : (v >= m ? v - m : v); }
+
+struct WarpSmem {
+    float4 xy[kStage / 2];     // pre-shifted (x_a, x_b, y_a, y_b) of slots 2p, 2p+1
+    float2 zz[kStage / 2];     // pre-shifted (z_a, z_b)
+    float4 raw[kStage];        // unshifted x, y, z; .w = type | shift code << 8
+    uint32_t mask[kGroups * 32];  // [group][lane]
+};
+
+struct Lane {
+    float4 h;     // home position (raw)
+    uint32_t tp;  // home type
+    float fx, fy, fz;
+    int count;
+};
+
+template <bool kUniformR>
+__device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float4 o, const float* s_force,
+                                           const float* s_inv_eff, const float* s_thr, bool generic)
+{
+    float dx = __fsub_rn(o.x, L.h.x);
+    float dy = __fsub_rn(o.y, L.h.y);
+    float dz = __fsub_rn(o.z, L.h.z);
+    const uint32_t wbits = __float_as_uint(o.w);
+    if (generic) {
+        dx = wrap_ref(dx, c.ext[0], c.half[0]);
+        dy = wrap_ref(dy, c.ext[1], c.half[1]);
+        dz = wrap_ref(dz, c.ext[2], c.half[2]);
+    } else {
+        const uint32_t code = wbits >> 8;
+        dx = __fadd_rn(dx, code_shift(code & 3u, c.ext[0]));
+        dy = __fadd_rn(dy, code_shift((code >> 2) & 3u, c.ext[1]));
+        dz = __fadd_rn(dz, code_shift((code >> 4) & 3u, c.ext[2]));
+    }
+    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    const float s = __fadd_rn(d2, 0.0001f);
+    const uint32_t pair = L.tp * kTableStride + (wbits & (kTableStride - 1));
+    const float thr = kUniformR ? c.thr_uniform : s_thr[pair];
+    if (s < thr) {
+        L.count++;
+        const float rs = rsqrtf(s);
+        const float dist = s * rs;
+        const float r = dist * (kUniformR ? c.inv_eff_uniform : s_inv_eff[pair]);
+        const float ex = __expf(c.neg_k * r * r);
+        const float net = fmaf(c.repulsion, ex, -c.attraction * r) * s_force[pair];
+        const float wgt = net * rs;
+        L.fx = fmaf(dx, wgt, L.fx);
+        L.fy = fmaf(dy, wgt, L.fy);
+        L.fz = fmaf(dz, wgt, L.fz);
+    }
+}
+
 template <bool kGeneric, bool kUniformR>
 __global__ void __launch_bounds__(kThreads)
     step_force_kernel(StepConsts c, const PairTables* __restrict__ tables, const float4* __restrict__ pos_sorted,
                       const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ vals_sorted,
-                      const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ cell_end,
-                      float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ acc,
-                      int* __restrict__ counts)
+                      const uint32_t* __restrict__ cell_off, const int2* __restrict__ items,
+                      const int* __restrict__ n_items, float4* __restrict__ pos, float4* __restrict__ vel,
+                      float4* __restrict__ acc, int* __restrict__ counts)
 {
     __shared__ float s_force[kTableSize];
-    __shared__ float s_eff[kTableSize];
-    __shared__ float s_thr[kTableSize];
+    __shared__ float s_inv_eff[kUniformR ? 1 : kTableSize];
+    __shared__ float s_thr[kUniformR ? 1 : kTableSize];
+    __shared__ WarpSmem s_warp[kWarps];
     const int T = c.num_types;
     for (int e = threadIdx.x; e < T * T; e += kThreads) {
-        int a = e / T, b = e - a * T;
-        int k = a * kTableStride + b;
+        const int a = e / T, b = e - a * T;
+        const int k = a * kTableStride + b;
         s_force[k] = tables->force[k];
-        s_eff[k] = tables->eff[k];
-        s_thr[k] = tables->threshold[k];
+        if (!kUniformR) {
+            s_inv_eff[k] = 1.0f / tables->eff[k];
+            s_thr[k] = tables->threshold[k];
+        }
     }
     __syncthreads();
 
-    const int t = blockIdx.x * kThreads + threadIdx.x;
-    if (t >= c.n) return;
-    const float4 h = pos_sorted[t];
-    const uint32_t tp = __float_as_uint(h.w) & (kTableStride - 1);
-    const uint32_t key = keys_sorted[t];
-    const int mx = c.grid.m[0], my = c.grid.m[1], mz = c.grid.m[2];
-    const int cx = (int)(key % (uint32_t)mx);
-    const int cy = (int)((key / (uint32_t)mx) % (uint32_t)my);
-    const int cz = (int)(key / (uint32_t)(mx * my));
-    // stencil extent per axis: a single layer when an axis has one cell
-    const int lo_x = mx > 1 ? -1 : 0, hi_x = mx > 1 ? 1 : 0;
-    const int lo_y = my > 1 ? -1 : 0, hi_y = my > 1 ? 1 : 0;
-    const int lo_z = mz > 1 ? -1 : 0, hi_z = mz > 1 ? 1 : 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int item = blockIdx.x * kWarps + warp;
+    if (item >= *n_items) return;
+    WarpSmem& w = s_warp[warp];
+    const int2 it = items[item];
+    const bool active = lane < it.y;
+    const int t = it.x + (active ? lane : 0);
+    Lane L;
+    L.h = pos_sorted[t];
+    L.tp = __float_as_uint(L.h.w) & (kTableStride - 1);
+    L.fx = L.fy = L.fz = 0.0f;
+    L.count = 0;
 
-    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
-    int count = 0;
-    for (int oz = lo_z; oz <= hi_z; oz++) {
-        int z = cz + oz;
-        float sz = 0.0f;
-        if (z < 0) { z += mz; sz = -c.ext[2]; }
-        else if (z >= mz) { z -= mz; sz = c.ext[2]; }
-        for (int oy = lo_y; oy <= hi_y; oy++) {
-            int y = cy + oy;
-            float sy = 0.0f;
-            if (y < 0) { y += my; sy = -c.ext[1]; }
-            else if (y >= my) { y -= my; sy = c.ext[1]; }
-            for (int ox = lo_x; ox <= hi_x; ox++) {
-                int x = cx + ox;
-                float sx = 0.0f;
-                if (x < 0) { x += mx; sx = -c.ext[0]; }
-                else if (x >= mx) { x -= mx; sx = c.ext[0]; }
-                const uint32_t cell = (uint32_t)((z * my + y) * mx + x);
-                const uint32_t j_end = cell_end[cell];
-                for (uint32_t j = cell_start[cell]; j < j_end; j++) {
-                    if (j == (uint32_t)t) continue;
-                    const float4 q = pos_sorted[j];
-                    float dx = __fsub_rn(q.x, h.x);
-                    float dy = __fsub_rn(q.y, h.y);
-                    float dz = __fsub_rn(q.z, h.z);
-                    if (kGeneric) {
-                        dx = wrap_ref(dx, c.ext[0], c.half[0]);
-                        dy = wrap_ref(dy, c.ext[1], c.half[1]);
-                        dz = wrap_ref(dz, c.ext[2], c.half[2]);
-                    } else {
-                        dx = __fadd_rn(dx, sx);
-                        dy = __fadd_rn(dy, sy);
-                        dz = __fadd_rn(dz, sz);
-                    }
-                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                    const float s = __fadd_rn(d2, 0.0001f);
-                    const uint32_t to = __float_as_uint(q.w) & (kTableStride - 1);
-                    const int pair = (int)(tp * kTableStride + to);
-                    const float thr = kUniformR ? c.thr_uniform : s_thr[pair];
-                    if (s < thr) {
-                        count++;
-                        const float eff = kUniformR ? c.eff_uniform : s_eff[pair];
-                        const float dist = __fsqrt_rn(s);
-                        const float r = __fdiv_rn(dist, eff);
-                        const float rep = __fmul_rn(c.repulsion, expf(__fmul_rn(__fmul_rn(c.neg_k, r), r)));
-                        const float att = __fmul_rn(c.attraction, r);
-                        const float net = __fmul_rn(__fsub_rn(rep, att), s_force[pair]);
-                        fx = __fadd_rn(fx, __fmul_rn(__fdiv_rn(dx, dist), net));
-                        fy = __fadd_rn(fy, __fmul_rn(__fdiv_rn(dy, dist), net));
-                        fz = __fadd_rn(fz, __fmul_rn(__fdiv_rn(dz, dist), net));
-                    }
-                }
+    const int mx = c.grid.m[0], my = c.grid.m[1], mz = c.grid.m[2];
+    const uint32_t key_first = keys_sorted[it.x];
+    const int x0 = (int)(key_first % (uint32_t)mx);
+    const int x1 = (int)(keys_sorted[it.x + it.y - 1] % (uint32_t)mx);
+    const int yc = (int)((key_first / (uint32_t)mx) % (uint32_t)my);
+    const int zc = (int)(key_first / (uint32_t)(mx * my));
+    const int hx = (int)(keys_sorted[t] % (uint32_t)mx);
+    // x sub-ranges whose union (range plus one cell each side) fits in the box
+    const int width = kGeneric ? mx : (mx - 2);
+    const int passes = kGeneric ? 1 : (x1 - x0 + width) / width;
+    const float thr_f = c.thr_filter;
+
+    for (int pass = 0; pass < passes; pass++) {
+        const int px0 = kGeneric ? x0 : x0 + pass * width;
+        const int px1 = kGeneric ? x1 : min(x1, px0 + width - 1);
+        const bool mine = active && (kGeneric || (hx >= px0 && hx <= px1));
+        // an idle home sits at -kFar: 2e30 from every candidate and from the +kFar padding slots
+        const float hxf = mine ? L.h.x : -kFar, hyf = mine ? L.h.y : -kFar, hzf = mine ? L.h.z : -kFar;
+
+        // segments: lane 2*row + half describes one contiguous range of the snapshot
+        const int xlo = mx > 1 ? px0 - 1 : 0;
+        const int xhi = mx > 1 ? min(px1 + 1, xlo + mx - 1) : 0;  // inclusive, at most mx cells
+        int seg_beg = 0, seg_len = 0;
+        uint32_t seg_code = 0;
+        const int ny = my > 1 ? 3 : 1, nz = mz > 1 ? 3 : 1;
+        const int nseg = 2 * ny * nz;
+        {
+            const int row = lane >> 1, half = lane & 1;
+            const int oy = ny > 1 ? (row % ny) - 1 : 0, oz = nz > 1 ? (row / ny) - 1 : 0;
+            const int yy = wrap_index(yc + oy, my), zz = wrap_index(zc + oz, mz);
+            const uint32_t cy = (yc + oy < 0) ? 1u : (yc + oy >= my ? 2u : 0u);
+            const uint32_t cz = (zc + oz < 0) ? 1u : (zc + oz >= mz ? 2u : 0u);
+            // split [xlo, xhi] at the box edge: half 0 is the in-box part, half 1 the wrapped part
+            int a = xlo, b = xhi;
+            uint32_t cx = 0u;
+            if (xlo < 0) {
+                if (half == 0) a = 0;
+                else { a = xlo + mx; b = mx - 1; cx = 1u; }
+            } else if (xhi >= mx) {
+                if (half == 0) b = mx - 1;
+                else { a = 0; b = xhi - mx; cx = 2u; }
+            } else if (half == 1) {
+                b = a - 1;
+            }
+            if (row < ny * nz && b >= a) {
+                const uint32_t base = (uint32_t)((zz * my + yy) * mx);
+                seg_beg = (int)cell_off[base + a];
+                seg_len = (int)cell_off[base + b + 1] - seg_beg;
+                seg_code = kGeneric ? 0u : (cx | (cy << 2) | (cz << 4));
             }
         }
+        int seg_pre = seg_len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, seg_pre, o);
+            if (lane >= o) seg_pre += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, seg_pre, 31);
+        seg_pre -= seg_len;
+
+        for (int base = 0; base < total; base += kStage) {
+            const int lim = min(kStage, total - base);
+            const int ngroups = (lim + 31) >> 5;
+            int own = -1;  // this lane's own slot in the batch (self exclusion)
+            // ---- stage [base, base + lim) of the concatenated segments
+            for (int sg = 0; sg < nseg; sg++) {
+                const int pre = __shfl_sync(0xffffffffu, seg_pre, sg);
+                const int len = __shfl_sync(0xffffffffu, seg_len, sg);
+                const int beg = __shfl_sync(0xffffffffu, seg_beg, sg);
+                const uint32_t code = __shfl_sync(0xffffffffu, seg_code, sg);
+                if (t >= beg && t < beg + len) {
+                    const int g = pre + (t - beg);
+                    if (g >= base && g < base + lim) own = g - base;
+                }
+                const int lo = max(pre, base), hi = min(pre + len, base + lim);
+                if (hi <= lo) continue;
+                const float sx = code_shift(code & 3u, c.ext[0]);
+                const float sy = code_shift((code >> 2) & 3u, c.ext[1]);
+                const float sz = code_shift(code >> 4, c.ext[2]);
+                for (int g = lo + lane; g < hi; g += 32) {
+                    const int slot = g - base;
+                    float4 p = pos_sorted[beg + (g - pre)];
+                    float* xy = reinterpret_cast<float*>(&w.xy[slot >> 1]);
+                    float* zv = reinterpret_cast<float*>(&w.zz[slot >> 1]);
+                    xy[slot & 1] = p.x + sx;
+                    xy[2 + (slot & 1)] = p.y + sy;
+                    zv[slot & 1] = p.z + sz;
+                    p.w = __uint_as_float((__float_as_uint(p.w) & 0xffu) | (code << 8));
+                    w.raw[slot] = p;
+                }
+            }
+            // padding up to a whole group: never passes the filter
+            for (int slot = lim + lane; slot < ngroups * 32; slot += 32) {
+                float* xy = reinterpret_cast<float*>(&w.xy[slot >> 1]);
+                float* zv = reinterpret_cast<float*>(&w.zz[slot >> 1]);
+                xy[slot & 1] = kFar;
+                xy[2 + (slot & 1)] = kFar;
+                zv[slot & 1] = kFar;
+            }
+            __syncwarp();
+
+            // ---- filter: one bit per candidate
+            if (kGeneric) {
+                for (int gi = 0; gi < ngroups; gi++) {
+                    uint32_t m = 0;
+                    for (int q = 0; q < 32; q++) {
+                        const int slot = gi * 32 + q;
+                        if (slot >= lim) break;
+                        const float4 o = w.raw[slot];
+                        const float dx = wrap_ref(o.x - hxf, c.ext[0], c.half[0]);
+                        const float dy = wrap_ref(o.y - hyf, c.ext[1], c.half[1]);
+                        const float dz = wrap_ref(o.z - hzf, c.ext[2], c.half[2]);
+                        const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                        if (d2 < thr_f) m |= 1u << q;
+                    }
+                    w.mask[gi * 32 + lane] = m;
+                }
+            } else {
+                const float2 nhx = make_float2(-hxf, -hxf), nhy = make_float2(-hyf, -hyf),
+                             nhz = make_float2(-hzf, -hzf);
+                for (int gi = 0; gi < ngroups; gi++) {
+                    uint32_t m = 0;
+#pragma unroll
+                    for (int p = 0; p < 16; p++) {
+                        const float4 a = w.xy[gi * 16 + p];
+                        const float2 b = w.zz[gi * 16 + p];
+                        const float2 dx = __fadd2_rn(make_float2(a.x, a.y), nhx);
+                        const float2 dy = __fadd2_rn(make_float2(a.z, a.w), nhy);
+                        const float2 dz = __fadd2_rn(b, nhz);
+                        float2 d2 = __fmul2_rn(dx, dx);
+                        d2 = __ffma2_rn(dy, dy, d2);
+                        d2 = __ffma2_rn(dz, dz, d2);
+                        if (d2.x < thr_f) m |= 1u << (2 * p);
+                        if (d2.y < thr_f) m |= 1u << (2 * p + 1);
+                    }
+                    w.mask[gi * 32 + lane] = m;
+                }
+            }
+            __syncwarp();
+
+            // ---- drain: exact test and force for every set bit
+            int gi = 0;
+            uint32_t m = w.mask[lane];
+            while (true) {
+                while (m == 0u && gi < ngroups - 1) {
+                    gi++;
+                    m = w.mask[gi * 32 + lane];
+                }
+                const bool has = m != 0u;
+                if (!__any_sync(0xffffffffu, has)) break;
+                if (has) {
+                    const int slot = gi * 32 + (__ffs(m) - 1);
+                    m &= m - 1u;
+                    if (slot != own)
+                        pair_force<kUniformR>(c, L, w.raw[slot], s_force, s_inv_eff, s_thr, kGeneric);
+                }
+            }
+            __syncwarp();
+        }
     }
+    if (!active) return;
 
     // density-adaptive scale and integrator (ParticleSimulation.cu:136-161)
     const uint32_t i = vals_sorted[t];
     const int prev = counts[i];
-    const float avg = __fmul_rn((float)(count + prev), 0.5f);
+    const float avg = __fmul_rn((float)(L.count + prev), 0.5f);
     const float density = fminf(__fdiv_rn(avg, (float)c.max_expected_neighbors), 1.0f);
     const float adapt = __fsub_rn(1.0f, __fmul_rn(__fsub_rn(1.0f, c.balance), density));
     const float scale = __fmul_rn(c.force_multiplier, adapt);
-    fx = __fmul_rn(fx, scale);
-    fy = __fmul_rn(fy, scale);
-    fz = __fmul_rn(fz, scale);
+    const float fx = __fmul_rn(L.fx, scale);
+    const float fy = __fmul_rn(L.fy, scale);
+    const float fz = __fmul_rn(L.fz, scale);
     const float4 v = vel[i];
     const float vx = __fadd_rn(__fmul_rn(v.x, c.friction), __fmul_rn(fx, c.delta_t));
     const float vy = __fadd_rn(__fmul_rn(v.y, c.friction), __fmul_rn(fy, c.delta_t));
     const float vz = __fadd_rn(__fmul_rn(v.z, c.friction), __fmul_rn(fz, c.delta_t));
-    float px = __fadd_rn(h.x, __fmul_rn(vx, c.delta_t));
-    float py = __fadd_rn(h.y, __fmul_rn(vy, c.delta_t));
-    float pz = __fadd_rn(h.z, __fmul_rn(vz, c.delta_t));
+    float px = __fadd_rn(L.h.x, __fmul_rn(vx, c.delta_t));
+    float py = __fadd_rn(L.h.y, __fmul_rn(vy, c.delta_t));
+    float pz = __fadd_rn(L.h.z, __fmul_rn(vz, c.delta_t));
     px = fmodf(__fadd_rn(px, c.ext[0]), c.ext[0]);
     py = fmodf(__fadd_rn(py, c.ext[1]), c.ext[1]);
     pz = fmodf(__fadd_rn(pz, c.ext[2]), c.ext[2]);
-    pos[i] = make_float4(px, py, pz, h.w);
+    pos[i] = make_float4(px, py, pz, L.h.w);
     vel[i] = make_float4(vx, vy, vz, 0.0f);
     acc[i] = make_float4(fx, fy, fz, 0.0f);
-    counts[i] = count;
+    counts[i] = L.count;
+}
+
+// Items: each row of cells (rows = (y, z) pairs) cut into chunks of at most
+// 32 sorted particles.  One block; rows are split into contiguous segments.
+__global__ void __launch_bounds__(1024)
+    plan_kernel(const uint32_t* __restrict__ cell_off, int mx, int rows, int2* __restrict__ items,
+                int* __restrict__ n_items)
+{
+    __shared__ uint32_t s_chunk[1024];
+    const int tid = threadIdx.x;
+    const int per = (rows + 1023) / 1024;
+    const int r0 = min(tid * per, rows), r1 = min(r0 + per, rows);
+    uint32_t chunks = 0;
+    for (int r = r0; r < r1; r++) {
+        const uint32_t cnt = cell_off[(r + 1) * mx] - cell_off[r * mx];
+        chunks += (cnt + 31u) / 32u;
+    }
+    s_chunk[tid] = chunks;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const uint32_t b = tid >= o ? s_chunk[tid - o] : 0u;
+        __syncthreads();
+        s_chunk[tid] += b;
+        __syncthreads();
+    }
+    uint32_t item = s_chunk[tid] - chunks;
+    for (int r = r0; r < r1; r++) {
+        const uint32_t start = cell_off[r * mx];
+        const uint32_t cnt = cell_off[(r + 1) * mx] - start;
+        for (uint32_t k = 0; k < cnt; k += 32u) items[item++] = make_int2((int)(start + k), (int)min(32u, cnt - k));
+    }
+    if (tid == 1023) *n_items = (int)s_chunk[1023];
 }
 
 }  // namespace
 
-cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
-                              const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_start,
-                              const uint32_t* cell_end, float4* pos, float4* vel, float4* acc, int* counts,
-                              cudaStream_t st)
+int max_step_items(int n, const Grid& g) { return (n + 31) / 32 + g.m[1] * g.m[2]; }
+
+int step_launches(int n) { return n > 0 ? 2 : 0; }
+
+cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, int2* items, int* n_items,
+                             cudaStream_t st)
 {
-    if (c.n <= 0) return cudaSuccess;
-    const int blocks = (c.n + kThreads - 1) / kThreads;
+    if (n <= 0) return cudaMemsetAsync(n_items, 0, sizeof(int), st);
+    plan_kernel<<<1, 1024, 0, st>>>(cell_off, g.m[0], g.m[1] * g.m[2], items, n_items);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
+                              const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
+                              const int2* items, const int* n_items, int max_items, float4* pos, float4* vel,
+                              float4* acc, int* counts, cudaStream_t st)
+{
+    if (c.n <= 0 || max_items <= 0) return cudaSuccess;
+    const int blocks = (max_items + kWarps - 1) / kWarps;
+#define CF_FORCE_LAUNCH(G, U)                                                                                   \
+    step_force_kernel<G, U><<<blocks, kThreads, 0, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted,       \
+                                                         cell_off, items, n_items, pos, vel, acc, counts)
     if (c.grid.generic) {
         if (c.uniform_r)
-            step_force_kernel<true, true><<<blocks, kThreads, 0, st>>>(c, tables, pos_sorted, keys_sorted,
-                                                                       vals_sorted, cell_start, cell_end, pos, vel,
-                                                                       acc, counts);
+            CF_FORCE_LAUNCH(true, true);
         else
-            step_force_kernel<true, false><<<blocks, kThreads, 0, st>>>(c, tables, pos_sorted, keys_sorted,
-                                                                        vals_sorted, cell_start, cell_end, pos, vel,
-                                                                        acc, counts);
+            CF_FORCE_LAUNCH(true, false);
     } else {
         if (c.uniform_r)
-            step_force_kernel<false, true><<<blocks, kThreads, 0, st>>>(c, tables, pos_sorted, keys_sorted,
-                                                                        vals_sorted, cell_start, cell_end, pos, vel,
-                                                                        acc, counts);
+            CF_FORCE_LAUNCH(false, true);
         else
-            step_force_kernel<false, false><<<blocks, kThreads, 0, st>>>(c, tables, pos_sorted, keys_sorted,
-                                                                         vals_sorted, cell_start, cell_end, pos,
-                                                                         vel, acc, counts);
+            CF_FORCE_LAUNCH(false, false);
     }
+#undef CF_FORCE_LAUNCH
     return cudaGetLastError();
 }
 

@@ -132,9 +132,13 @@ void cfo_step_f32(int n, const float* pos, const float* vel, const uint32_t* typ
 
 /*
  * The same step in double precision from the same FP32 inputs, for error
- * reports.  Also returns, per particle, mag[i] = scale * sum_j |net_j|: the
- * size of the terms whose sum is the force, which bounds the rounding error
- * any summation order can make.  ParticleSimulation.cu:78-165.
+ * reports.  Also returns, per particle,
+ *     mag[i] = |scale| * sum_j |F_j| * (rep * exp(-k r_j^2) + att * r_j),
+ * the size of the quantities whose rounded combination is the force: each
+ * term is a difference (repulsion minus attraction, which cancels near their
+ * crossing) and the terms are summed, so any evaluation order or few-ulp
+ * function error moves the result by a small multiple of this, not of the
+ * (possibly cancelled) result.  ParticleSimulation.cu:78-165.
  */
 void cfo_step_f64(int n, const float* pos, const float* vel, const uint32_t* type, const int* cnt_in, const float* F,
                   const float* rb, const cfo_params* p, double* pos_out, double* vel_out, double* acc_out,
@@ -164,12 +168,14 @@ void cfo_step_f64(int n, const float* pos, const float* vel, const uint32_t* typ
             if (dist < eff) {
                 count++;
                 double r_ = dist / eff;
-                double net = ((double)p->repulsion * exp(-(double)p->k * r_ * r_) - (double)p->attraction * r_) *
-                             (double)F[tp * (uint32_t)p->num_types + to];
+                double rep = (double)p->repulsion * exp(-(double)p->k * r_ * r_);
+                double att = (double)p->attraction * r_;
+                double fv = (double)F[tp * (uint32_t)p->num_types + to];
+                double net = (rep - att) * fv;
                 fx += dx / dist * net;
                 fy += dy / dist * net;
                 fz += dz / dist * net;
-                sum_abs += fabs(net);
+                sum_abs += (fabs(rep) + fabs(att)) * fabs(fv);
             }
         }
         double avg = (count + cnt_in[i]) * 0.5;

@@ -3,10 +3,13 @@
 Tolerances (FP32, one step, library vs the reference's FP32 step):
   counts       bit-exact
   acceleration |a - a_ref| <= 1e-5 * m_i per component, m_i = the FP64
-               oracle's scale * sum_j |net_j|: the size of the terms whose
-               sum is the force.  Summation order (cell order against index
-               order) and CUDA's expf (2 ulp) move the sum by a few ulp of
-               those terms, never of the (possibly cancelled) total.
+               oracle's |scale| * sum_j |F_j| (rep e^{-k r^2} + att r): the
+               size of the quantities whose rounded combination is the force
+               (each term is a repulsion-minus-attraction difference that
+               cancels near r ~ 0.37, and the terms are summed).  Summation
+               order (cell order against index order) and few-ulp rsqrt/exp
+               approximations move the result by a few ulp of those
+               quantities, never of the (possibly cancelled) result.
   velocity     |v - v_ref| <= 1e-5 * (|v_ref| + dt * m_i)
   position     minimum-image |p - p_ref| <= 1e-5 * |p_ref| + 2 ulp(extent)
 """
