@@ -326,6 +326,7 @@ int prepare_step(cf_world* w, const cf_step_params* p, StepConsts* c)
     c->ext[2] = p->canvas_depth;
     for (int a = 0; a < 3; a++) c->half[a] = c->ext[a] * 0.5f;
     c->inv_eff_uniform = 1.0f / c->eff_uniform;
+    c->stage = w->force_stage;
     c->thr_filter = filter_bound(thr_max, std::max(c->ext[0], std::max(c->ext[1], c->ext[2])));
     c->grid = choose_step_grid(c->ext, r_cut, kMaxCells);
     c->n = w->n;
@@ -607,6 +608,8 @@ int cf_create(int n, int num_types, float w_, float h_, float d_, uint64_t seed,
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemsetAsync"));
     e = dev_alloc(&w->tables, 1);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(tables)"));
+    e = configure_step_force();
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaFuncSetAttribute(step_force_kernel)"));
     int rc = alloc_particles(w);
     if (rc) return bail(rc);
     // ParticleSimulation.cu:430-434: particles, force table (0.28, -0.20, 1.0), radius table
@@ -934,6 +937,92 @@ int cf_step(cf_world* w, const cf_step_params* p, int nsteps)
         }
     }
     return CF_OK;
+}
+
+int cf_set_force_stage(cf_world* w, int stage)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (stage != 256 && stage != 512) return fail(CF_ERR_INVALID, "force stage must be 256 or 512");
+    w->force_stage = stage;
+    return CF_OK;
+}
+
+int cf_autotune_step(cf_world* w, const cf_step_params* p, int steps, int* chosen_stage)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (steps < 1) steps = 1;
+    const size_t n = (size_t)w->n;
+    if (n == 0) return CF_OK;
+    // the trial steps must leave the world as it was: save the state
+    float4 *pos = nullptr, *vel = nullptr, *acc = nullptr;
+    int* cnt = nullptr;
+    CF_CUDA(dev_alloc(&pos, n));
+    CF_CUDA(dev_alloc(&vel, n));
+    CF_CUDA(dev_alloc(&acc, n));
+    CF_CUDA(dev_alloc(&cnt, n));
+    auto save = [&](bool to_backup) -> cudaError_t {
+        cudaError_t e = cudaSuccess;
+        const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+        if (to_backup) {
+            e = cudaMemcpyAsync(pos, w->pos, 16 * n, k, w->stream);
+            if (!e) e = cudaMemcpyAsync(vel, w->vel, 16 * n, k, w->stream);
+            if (!e) e = cudaMemcpyAsync(acc, w->acc, 16 * n, k, w->stream);
+            if (!e) e = cudaMemcpyAsync(cnt, w->counts, 4 * n, k, w->stream);
+        } else {
+            e = cudaMemcpyAsync(w->pos, pos, 16 * n, k, w->stream);
+            if (!e) e = cudaMemcpyAsync(w->vel, vel, 16 * n, k, w->stream);
+            if (!e) e = cudaMemcpyAsync(w->acc, acc, 16 * n, k, w->stream);
+            if (!e) e = cudaMemcpyAsync(w->counts, cnt, 4 * n, k, w->stream);
+        }
+        return e;
+    };
+    const int candidates[2] = {256, 512};
+    float best_ms = 1e30f;
+    int best = w->force_stage;
+    const int saved_stage = w->force_stage;
+    const bool saved_prof = w->profiling;
+    w->profiling = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (!e) e = cudaEventCreate(&e1);
+    if (!e) e = save(true);
+    for (int k = 0; k < 2 && !e && rc == CF_OK; k++) {
+        w->force_stage = candidates[k];
+        rc = cf_step(w, p, 1);  // capture and warm
+        if (rc) break;
+        e = cudaEventRecord(e0, w->stream);
+        if (!e) rc = cf_step(w, p, steps);
+        if (!e && !rc) e = cudaEventRecord(e1, w->stream);
+        if (!e && !rc) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (!e && !rc) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (!e && !rc && ms < best_ms) {
+            best_ms = ms;
+            best = candidates[k];
+        }
+        if (!e) e = save(false);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(w->stream);
+    dev_free(pos);
+    dev_free(vel);
+    dev_free(acc);
+    dev_free(cnt);
+    w->profiling = saved_prof;
+    if (rc) {
+        w->force_stage = saved_stage;
+        return rc;
+    }
+    if (e) {
+        w->force_stage = saved_stage;
+        return cuda_fail(e, "cf_autotune_step");
+    }
+    w->force_stage = best;
+    if (chosen_stage) *chosen_stage = best;
+    return sync_and_check(w);
 }
 
 int cf_profile_enable(cf_world* w, int on)

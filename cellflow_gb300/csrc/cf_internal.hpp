@@ -62,6 +62,7 @@ struct StepConsts {
     float thr_uniform;
     float inv_eff_uniform;
     float thr_filter;  // squared-distance bound of the approximate pre-test (>= every exact pass)
+    int stage;         // candidates staged per batch by the force kernel (256 or 512)
     float repulsion, attraction, neg_k, balance, force_multiplier, delta_t, friction;
     int max_expected_neighbors;
 };
@@ -135,6 +136,7 @@ struct cf_world {
     cf::StepConsts graph_key[2];
     const void* graph_bufs[2] = {nullptr, nullptr};
     bool use_graphs = true;
+    int force_stage = 512;  // force-kernel staging batch, chosen by cf_autotune_step
 };
 
 namespace cf {
@@ -163,6 +165,7 @@ cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, int
                              cudaStream_t st);
 int max_step_items(int n, const Grid& g);
 int step_launches(int n);
+cudaError_t configure_step_force();
 cudaError_t launch_scan_exclusive(const uint32_t* in, uint32_t* out, int n, uint32_t* tmp, size_t tmp_cap,
                                   cudaStream_t st);
 size_t scan_tmp_entries(int n);

@@ -42,8 +42,6 @@ namespace {
 
 constexpr int kWarps = 4;
 constexpr int kThreads = 32 * kWarps;
-constexpr int kStage = 256;  // staged candidates per batch (multiple of 32)
-constexpr int kGroups = kStage / 32;
 constexpr float kFar = 1e30f;  // padding slots sit at +kFar, idle homes at -kFar
 
 __device__ __forceinline__ float wrap_ref(float d, float ext, float half)
@@ -62,11 +60,13 @@ __device__ __forceinline__ float code_shift(uint32_t code, float ext)
 
 __device__ __forceinline__ int wrap_index(int v, int m) { return v < 0 ? v + m : (v >= m ? v - m : v); }
 
+// Per-warp staging area, kStage candidates (a multiple of 32) per batch.
+template <int kStage>
 struct WarpSmem {
-    float4 xy[kStage / 2];     // pre-shifted (x_a, x_b, y_a, y_b) of slots 2p, 2p+1
-    float2 zz[kStage / 2];     // pre-shifted (z_a, z_b)
-    float4 raw[kStage];        // unshifted x, y, z; .w = type | shift code << 8
-    uint32_t mask[kGroups * 32];  // [group][lane]
+    float4 xy[kStage / 2];           // pre-shifted (x_a, x_b, y_a, y_b) of slots 2p, 2p+1
+    float2 zz[kStage / 2];           // pre-shifted (z_a, z_b)
+    float4 raw[kStage];              // unshifted x, y, z; .w = type | shift code << 8
+    uint32_t mask[(kStage / 32) * 32];  // [group][lane]
 };
 
 struct Lane {
@@ -78,7 +78,8 @@ struct Lane {
 
 template <bool kUniformR>
 __device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float4 o, const float* s_force,
-                                           const float* s_inv_eff, const float* s_thr, bool generic)
+                                           const float* s_inv_eff, const float* s_thr, const float4* s_shift,
+                                           bool generic)
 {
     float dx = __fsub_rn(o.x, L.h.x);
     float dy = __fsub_rn(o.y, L.h.y);
@@ -89,10 +90,10 @@ __device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float4 
         dy = wrap_ref(dy, c.ext[1], c.half[1]);
         dz = wrap_ref(dz, c.ext[2], c.half[2]);
     } else {
-        const uint32_t code = wbits >> 8;
-        dx = __fadd_rn(dx, code_shift(code & 3u, c.ext[0]));
-        dy = __fadd_rn(dy, code_shift((code >> 2) & 3u, c.ext[1]));
-        dz = __fadd_rn(dz, code_shift((code >> 4) & 3u, c.ext[2]));
+        const float4 sh = s_shift[(wbits >> 8) & 63u];
+        dx = __fadd_rn(dx, sh.x);
+        dy = __fadd_rn(dy, sh.y);
+        dz = __fadd_rn(dz, sh.z);
     }
     const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
     const float s = __fadd_rn(d2, 0.0001f);
@@ -112,7 +113,7 @@ __device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float4 
     }
 }
 
-template <bool kGeneric, bool kUniformR>
+template <int kStage, bool kGeneric, bool kUniformR>
 __global__ void __launch_bounds__(kThreads)
     step_force_kernel(StepConsts c, const PairTables* __restrict__ tables, const float4* __restrict__ pos_sorted,
                       const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ vals_sorted,
@@ -123,7 +124,8 @@ __global__ void __launch_bounds__(kThreads)
     __shared__ float s_force[kTableSize];
     __shared__ float s_inv_eff[kUniformR ? 1 : kTableSize];
     __shared__ float s_thr[kUniformR ? 1 : kTableSize];
-    __shared__ WarpSmem s_warp[kWarps];
+    __shared__ float4 s_shift[64];  // periodic shift of each shift code
+    extern __shared__ __align__(16) unsigned char s_dyn[];
     const int T = c.num_types;
     for (int e = threadIdx.x; e < T * T; e += kThreads) {
         const int a = e / T, b = e - a * T;
@@ -134,12 +136,17 @@ __global__ void __launch_bounds__(kThreads)
             s_thr[k] = tables->threshold[k];
         }
     }
+    if (threadIdx.x < 64) {
+        const uint32_t code = threadIdx.x;
+        s_shift[code] = make_float4(code_shift(code & 3u, c.ext[0]), code_shift((code >> 2) & 3u, c.ext[1]),
+                                    code_shift((code >> 4) & 3u, c.ext[2]), 0.0f);
+    }
     __syncthreads();
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int item = blockIdx.x * kWarps + warp;
     if (item >= *n_items) return;
-    WarpSmem& w = s_warp[warp];
+    WarpSmem<kStage>& w = reinterpret_cast<WarpSmem<kStage>*>(s_dyn)[warp];
     const int2 it = items[item];
     const bool active = lane < it.y;
     const int t = it.x + (active ? lane : 0);
@@ -303,7 +310,7 @@ __global__ void __launch_bounds__(kThreads)
                     const int slot = gi * 32 + (__ffs(m) - 1);
                     m &= m - 1u;
                     if (slot != own)
-                        pair_force<kUniformR>(c, L, w.raw[slot], s_force, s_inv_eff, s_thr, kGeneric);
+                        pair_force<kUniformR>(c, L, w.raw[slot], s_force, s_inv_eff, s_thr, s_shift, kGeneric);
                 }
             }
             __syncwarp();
@@ -383,16 +390,35 @@ cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, int
     return cudaGetLastError();
 }
 
-cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
-                              const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
-                              const int2* items, const int* n_items, int max_items, float4* pos, float4* vel,
-                              float4* acc, int* counts, cudaStream_t st)
+namespace {
+
+template <int S, bool G, bool U>
+cudaError_t configure_variant()
 {
-    if (c.n <= 0 || max_items <= 0) return cudaSuccess;
-    const int blocks = (max_items + kWarps - 1) / kWarps;
-#define CF_FORCE_LAUNCH(G, U)                                                                                   \
-    step_force_kernel<G, U><<<blocks, kThreads, 0, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted,       \
-                                                         cell_off, items, n_items, pos, vel, acc, counts)
+    return cudaFuncSetAttribute(step_force_kernel<S, G, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(WarpSmem<S>) * kWarps));
+}
+
+template <int S>
+cudaError_t configure_stage()
+{
+    cudaError_t e = configure_variant<S, false, false>();
+    if (e == cudaSuccess) e = configure_variant<S, false, true>();
+    if (e == cudaSuccess) e = configure_variant<S, true, false>();
+    if (e == cudaSuccess) e = configure_variant<S, true, true>();
+    return e;
+}
+
+template <int S>
+cudaError_t launch_stage(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
+                         const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
+                         const int2* items, const int* n_items, int blocks, float4* pos, float4* vel, float4* acc,
+                         int* counts, cudaStream_t st)
+{
+    const size_t smem = sizeof(WarpSmem<S>) * kWarps;
+#define CF_FORCE_LAUNCH(G, U)                                                                                     \
+    step_force_kernel<S, G, U><<<blocks, kThreads, smem, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted,   \
+                                                               cell_off, items, n_items, pos, vel, acc, counts)
     if (c.grid.generic) {
         if (c.uniform_r)
             CF_FORCE_LAUNCH(true, true);
@@ -406,6 +432,31 @@ cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, con
     }
 #undef CF_FORCE_LAUNCH
     return cudaGetLastError();
+}
+
+}  // namespace
+
+// Opt the force kernels into their dynamic shared memory (outside any
+// stream capture).
+cudaError_t configure_step_force()
+{
+    cudaError_t e = configure_stage<256>();
+    if (e == cudaSuccess) e = configure_stage<512>();
+    return e;
+}
+
+cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
+                              const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
+                              const int2* items, const int* n_items, int max_items, float4* pos, float4* vel,
+                              float4* acc, int* counts, cudaStream_t st)
+{
+    if (c.n <= 0 || max_items <= 0) return cudaSuccess;
+    const int blocks = (max_items + kWarps - 1) / kWarps;
+    if (c.stage == 256)
+        return launch_stage<256>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items, blocks,
+                                 pos, vel, acc, counts, st);
+    return launch_stage<512>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items, blocks, pos,
+                             vel, acc, counts, st);
 }
 
 }  // namespace cf

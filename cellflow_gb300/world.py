@@ -209,6 +209,16 @@ class ParticleSimulation:
         p = params.to_c()
         check(self._lib.cf_step(self._h, C.byref(p), steps), "cf_step")
 
+    def autotune(self, params: SimulationParams, steps: int = 3) -> int:
+        """Pick the force kernel's staging batch by timing trial steps; the state is restored."""
+        p = params.to_c()
+        chosen = C.c_int()
+        check(self._lib.cf_autotune_step(self._h, C.byref(p), steps, C.byref(chosen)), "cf_autotune_step")
+        return chosen.value
+
+    def set_force_stage(self, stage: int) -> None:
+        check(self._lib.cf_set_force_stage(self._h, stage), "cf_set_force_stage")
+
     def grid(self, params: SimulationParams) -> GridInfo:
         g = GridInfo()
         p = params.to_c()

@@ -180,6 +180,14 @@ float cf_lfo_ratio(float ratio, float lfo_a, float lfo_s, float t_seconds);
  * builds the cell list, computes forces, neighbour counts and the
  * density-adaptive scale, integrates and wraps.  Asynchronous. */
 int cf_step(cf_world* w, const cf_step_params* p, int nsteps);
+/* Autotuner of the step (no counterpart in the reference): runs `steps`
+ * trial steps with each staging batch size of the force kernel (256 and 512
+ * candidates per warp batch), restores the particle state, keeps the faster
+ * variant for later steps and returns it in *chosen_stage.  Results are
+ * identical whichever variant runs; only speed differs. */
+int cf_autotune_step(cf_world* w, const cf_step_params* p, int steps, int* chosen_stage);
+/* Set the staging batch directly (256 or 512). */
+int cf_set_force_stage(cf_world* w, int stage);
 /* The grid cf_step would use for these parameters. */
 int cf_get_grid(cf_world* w, const cf_step_params* p, cf_grid_info* out);
 /* Build the cell list of the current positions with the step's grid and
