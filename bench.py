@@ -249,7 +249,7 @@ def run_gb300(args, rank, world, local):
         if world > 1:
             torch.distributed.barrier()
 
-    force_stage = sim.autotune(params, 3)  # picks the staging batch; restores the state
+    force_variant = sim.autotune(params, 3)  # picks the force-kernel variant; restores the state
     for _ in range(args.warmup):
         sim.simulate(params, 1)
     sim.sync()
@@ -340,7 +340,7 @@ def run_gb300(args, rank, world, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Philox4x32-10), shapes and distributions of the workload",
-            "config": dict(workload_config(w), force_stage=force_stage),
+            "config": dict(workload_config(w), force_variant=force_variant),
             "roofline": {
                 "kernel": "step_force_kernel (force + density + integrator)", "bound": "fp32",
                 "achieved": achieved_tflops, "peak": peak_fp32.value, "unit": "TFLOP/s",

@@ -141,7 +141,7 @@ _SIGNATURES = {
     "cf_step": (C.c_int, [_W, _P(StepParams), C.c_int]),
     "cf_get_grid": (C.c_int, [_W, _P(StepParams), _P(GridInfo)]),
     "cf_autotune_step": (C.c_int, [_W, _P(StepParams), C.c_int, _P(C.c_int)]),
-    "cf_set_force_stage": (C.c_int, [_W, C.c_int]),
+    "cf_set_force_variant": (C.c_int, [_W, C.c_int]),
     "cf_debug_cell_list": (
         C.c_int,
         [_W, _P(StepParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],

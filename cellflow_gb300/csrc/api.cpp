@@ -232,12 +232,15 @@ int update_pair_tables(cf_world* w, const cf_step_params* p, float* r_cut, int* 
 {
     const int T = w->num_types;
     PairTables& h = w->host_tables;
+    const float max_ext = std::max(p->canvas_width, std::max(p->canvas_height, p->canvas_depth));
     bool changed = w->uploaded_version != w->table_version || w->uploaded_radius != p->radius ||
-                   w->uploaded_ratio != p->ratio_with_lfo || w->uploaded_types != T;
+                   w->uploaded_ratio != p->ratio_with_lfo || w->uploaded_types != T ||
+                   w->uploaded_extent != max_ext;
     if (changed) {
         std::fill(std::begin(h.force), std::end(h.force), 0.0f);
         std::fill(std::begin(h.eff), std::end(h.eff), 0.0f);
         std::fill(std::begin(h.threshold), std::end(h.threshold), 0.0f);
+        std::fill(std::begin(h.threshold_lo), std::end(h.threshold_lo), 0.0f);
         for (int a = 0; a < T; a++) {
             for (int b = 0; b < T; b++) {
                 const float ra = p->radius * (1.0f + w->radio[a] * p->ratio_with_lfo);
@@ -247,6 +250,7 @@ int update_pair_tables(cf_world* w, const cf_step_params* p, float* r_cut, int* 
                 h.force[k] = w->table[a * T + b];
                 h.eff[k] = eff;
                 h.threshold[k] = sqrt_threshold(eff);
+                h.threshold_lo[k] = certain_bound(h.threshold[k], max_ext);
             }
         }
         CF_CUDA(cudaMemcpyAsync(w->tables, &h, sizeof(PairTables), cudaMemcpyHostToDevice, w->stream));
@@ -254,6 +258,7 @@ int update_pair_tables(cf_world* w, const cf_step_params* p, float* r_cut, int* 
         w->uploaded_radius = p->radius;
         w->uploaded_ratio = p->ratio_with_lfo;
         w->uploaded_types = T;
+        w->uploaded_extent = max_ext;
     }
     float thr_max = 0.0f;
     bool uniform = true;
@@ -297,6 +302,23 @@ int build_cell_list(cf_world* w, const Grid& g, const float* ext, int* which)
     return CF_OK;
 }
 
+// Bound below which the force kernel's contracted squared distance proves the
+// exact test passes: d2a < bound  implies  fl(d2e + 1e-4) < t, with the same
+// displacement slack as filter_bound.  Pairs between this and the filter
+// bound take the exact test.
+float certain_bound_impl(float thr, float max_extent)
+{
+    if (std::isinf(thr)) return INFINITY;
+    const double b = (double)thr * (1.0 - 0x1p-22) - (double)0.0001f;
+    if (!(b > 0.0)) return 0.0f;
+    int ex = 0;
+    std::frexp(2.0 * (double)max_extent, &ex);
+    const double delta = 2.0 * std::ldexp(1.0, ex - 24);
+    const double lo = b - 3.47 * delta * std::sqrt(b) - 3.0 * delta * delta - 0x1p-20 * b;
+    if (!(lo > 0.0)) return 0.0f;
+    return nextafterf((float)lo, 0.0f);
+}
+
 // Bound for the force kernel's approximate pre-test: every pair whose exact
 // test fl(d^2 + 1e-4) < t passes fl(fma-contracted d^2 of a pre-shifted
 // displacement) < bound.  The displacements differ by at most delta per axis
@@ -326,7 +348,8 @@ int prepare_step(cf_world* w, const cf_step_params* p, StepConsts* c)
     c->ext[2] = p->canvas_depth;
     for (int a = 0; a < 3; a++) c->half[a] = c->ext[a] * 0.5f;
     c->inv_eff_uniform = 1.0f / c->eff_uniform;
-    c->stage = w->force_stage;
+    c->thr_lo_uniform = w->host_tables.threshold_lo[0];
+    c->variant = w->force_variant;
     c->thr_filter = filter_bound(thr_max, std::max(c->ext[0], std::max(c->ext[1], c->ext[2])));
     c->grid = choose_step_grid(c->ext, r_cut, kMaxCells);
     c->n = w->n;
@@ -451,6 +474,8 @@ float sqrt_threshold(float eff)
     }
     return t;
 }
+
+float certain_bound(float threshold, float max_extent) { return certain_bound_impl(threshold, max_extent); }
 
 // Largest true distance a pair can have and still pass fl(d^2 + 1e-4) < t,
 // with slack for the rounding of the displacement, the squares and sums.
@@ -939,16 +964,16 @@ int cf_step(cf_world* w, const cf_step_params* p, int nsteps)
     return CF_OK;
 }
 
-int cf_set_force_stage(cf_world* w, int stage)
+int cf_set_force_variant(cf_world* w, int variant)
 {
     int rc = check_world(w);
     if (rc) return rc;
-    if (stage != 256 && stage != 512) return fail(CF_ERR_INVALID, "force stage must be 256 or 512");
-    w->force_stage = stage;
+    if (variant < 0 || variant >= CF_FORCE_VARIANTS) return fail(CF_ERR_INVALID, "force variant must be 0, 1 or 2");
+    w->force_variant = variant;
     return CF_OK;
 }
 
-int cf_autotune_step(cf_world* w, const cf_step_params* p, int steps, int* chosen_stage)
+int cf_autotune_step(cf_world* w, const cf_step_params* p, int steps, int* chosen_variant)
 {
     int rc = check_world(w);
     if (rc) return rc;
@@ -978,18 +1003,17 @@ int cf_autotune_step(cf_world* w, const cf_step_params* p, int steps, int* chose
         }
         return e;
     };
-    const int candidates[2] = {256, 512};
     float best_ms = 1e30f;
-    int best = w->force_stage;
-    const int saved_stage = w->force_stage;
+    int best = w->force_variant;
+    const int saved_variant = w->force_variant;
     const bool saved_prof = w->profiling;
     w->profiling = false;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t e = cudaEventCreate(&e0);
     if (!e) e = cudaEventCreate(&e1);
     if (!e) e = save(true);
-    for (int k = 0; k < 2 && !e && rc == CF_OK; k++) {
-        w->force_stage = candidates[k];
+    for (int k = 0; k < CF_FORCE_VARIANTS && !e && rc == CF_OK; k++) {
+        w->force_variant = k;
         rc = cf_step(w, p, 1);  // capture and warm
         if (rc) break;
         e = cudaEventRecord(e0, w->stream);
@@ -1000,7 +1024,7 @@ int cf_autotune_step(cf_world* w, const cf_step_params* p, int steps, int* chose
         if (!e && !rc) e = cudaEventElapsedTime(&ms, e0, e1);
         if (!e && !rc && ms < best_ms) {
             best_ms = ms;
-            best = candidates[k];
+            best = k;
         }
         if (!e) e = save(false);
     }
@@ -1013,15 +1037,15 @@ int cf_autotune_step(cf_world* w, const cf_step_params* p, int steps, int* chose
     dev_free(cnt);
     w->profiling = saved_prof;
     if (rc) {
-        w->force_stage = saved_stage;
+        w->force_variant = saved_variant;
         return rc;
     }
     if (e) {
-        w->force_stage = saved_stage;
+        w->force_variant = saved_variant;
         return cuda_fail(e, "cf_autotune_step");
     }
-    w->force_stage = best;
-    if (chosen_stage) *chosen_stage = best;
+    w->force_variant = best;
+    if (chosen_variant) *chosen_variant = best;
     return sync_and_check(w);
 }
 

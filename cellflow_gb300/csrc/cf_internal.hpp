@@ -17,7 +17,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/cellflow.h"
+#include "cellflow.h"
 
 namespace cf {
 
@@ -35,9 +35,10 @@ constexpr int kTableSize = CF_MAX_TYPES * CF_MAX_TYPES;
 
 // Per-pair tables for a step, uploaded together.
 struct PairTables {
-    float force[kTableSize];      // F[self][other]
-    float eff[kTableSize];        // effective radius (ParticleSimulation.cu:108-110)
-    float threshold[kTableSize];  // smallest float t with sqrtf(t) >= eff
+    float force[kTableSize];         // F[self][other]
+    float eff[kTableSize];           // effective radius (ParticleSimulation.cu:108-110)
+    float threshold[kTableSize];     // smallest float t with sqrtf(t) >= eff
+    float threshold_lo[kTableSize];  // contracted d^2 below this interacts for certain
 };
 
 // Grid of one cell list.
@@ -61,8 +62,9 @@ struct StepConsts {
     float eff_uniform;
     float thr_uniform;
     float inv_eff_uniform;
+    float thr_lo_uniform;  // contracted d^2 below this interacts for certain (uniform radius)
     float thr_filter;  // squared-distance bound of the approximate pre-test (>= every exact pass)
-    int stage;         // candidates staged per batch by the force kernel (256 or 512)
+    int variant;       // force-kernel variant (staging batch, occupancy), see cf_set_force_variant
     float repulsion, attraction, neg_k, balance, force_multiplier, delta_t, friction;
     int max_expected_neighbors;
 };
@@ -124,6 +126,7 @@ struct cf_world {
     float uploaded_radius = -1.0f;
     float uploaded_ratio = 0.0f;
     int uploaded_types = -1;
+    float uploaded_extent = -1.0f;
     cf::PairTables host_tables;
     // phase profiling (cf_profile_enable): events start / after cell list / after force
     bool profiling = false;
@@ -136,7 +139,7 @@ struct cf_world {
     cf::StepConsts graph_key[2];
     const void* graph_bufs[2] = {nullptr, nullptr};
     bool use_graphs = true;
-    int force_stage = 512;  // force-kernel staging batch, chosen by cf_autotune_step
+    int force_variant = 0;  // force-kernel variant, chosen by cf_autotune_step
 };
 
 namespace cf {
@@ -197,5 +200,6 @@ Grid choose_prox_grid(const float* ext, float distance, int max_cells);
 Grid canonical_grid(const float* ext, float r_max);
 float sqrt_threshold(float eff);
 float cutoff_distance(float threshold);
+float certain_bound(float threshold, float max_extent);
 
 }  // namespace cf

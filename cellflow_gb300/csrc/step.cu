@@ -6,32 +6,34 @@
 // an item are the particles of the union of its homes' 27-cell stencils:
 // 9 rows, each a run of consecutive cells, i.e. one contiguous range of the
 // sorted snapshot (two where the run wraps around the box in x).  The warp
-// copies those ranges into shared memory with coalesced loads, 256 at a
-// time, and every lane tests every staged candidate (broadcast reads).
+// copies those ranges into shared memory, 256 or 512 at a time (chosen by
+// the autotuner), with their periodic shift already applied, and every lane
+// tests every staged candidate (broadcast reads).
 //
 // Per batch of staged candidates, two phases per lane:
 //   Filter: squared distances of two candidates per instruction (packed f32x2
-//     add/mul/fma of sm_100+) from the lane's home to candidates staged with
-//     their segment's periodic shift already applied, against a bound that
-//     is >= the exact test for every pair.  The result is one 32-bit mask per
-//     32 candidates; about 85% of pairs fail here.
-//   Drain: for every set bit, the reference's exact test on the unshifted
-//     coordinates and, when it passes, the force term.
+//     add/mul/fma of sm_100+) against a bound that is >= the exact test for
+//     every pair; one 32-bit mask per 32 candidates.  ~85% of pairs stop here.
+//   Drain: for every set bit, the same contracted distance again; pairs whose
+//     distance is below a second bound (<= the exact test for every pair)
+//     interact for certain, and only the rare pairs between the two bounds
+//     (a band ~1e-6 wide) take the reference's exact test on the unshifted
+//     coordinates.  Interacting pairs add their force term.
 //
 // Exactness (cuda-native/src/ParticleSimulation.cu:86-165):
 //   - the neighbour test is the reference's: d^2 = (dx*dx + dy*dy) + dz*dz and
 //     s = d^2 + 1e-4 rounded as the reference (compiled without contraction)
 //     rounds them, and sqrtf(s) < eff is replaced by the equivalent s < t,
-//     t the smallest float whose correctly rounded square root is >= eff;
-//     neighbour counts match bit for bit;
+//     t the smallest float whose correctly rounded square root is >= eff.
+//     The two bounds bracket that test, so neighbour counts match bit for bit;
 //   - a displacement is wrapped like the reference (subtract the extent where
 //     its test fires).  With at least 5 cells per axis that is exactly the
 //     stencil cells across the box edge: the union of an item spans at most
-//     the box width in x, so every staged range has one shift for every
-//     lane, added after the subtraction as the reference does.  With fewer
-//     cells both phases run the reference's tests per candidate;
-//   - force terms use rsqrt and exp approximations (a few ulp) instead of the
-//     reference's sqrtf, divisions and expf; the sum runs in cell order.
+//     the box width in x, so every staged range has one shift for every lane,
+//     added after the subtraction (exact path) as the reference does.  With
+//     fewer cells both phases run the reference's tests per candidate;
+//   - force terms use rsqrt and exp approximations (a few ulp) and the
+//     contracted distance; the sum runs in cell order.
 //   The density factor, integrator and wrap are the reference's operations.
 #include <cuda_runtime.h>
 
@@ -43,6 +45,8 @@ namespace {
 constexpr int kWarps = 4;
 constexpr int kThreads = 32 * kWarps;
 constexpr float kFar = 1e30f;  // padding slots sit at +kFar, idle homes at -kFar
+constexpr int kTypeShift = 27; // staged meta: sorted index | type << 27
+constexpr uint32_t kIndexMask = (1u << kTypeShift) - 1u;
 
 __device__ __forceinline__ float wrap_ref(float d, float ext, float half)
 {
@@ -58,14 +62,21 @@ __device__ __forceinline__ float code_shift(uint32_t code, float ext)
     return code == 1u ? -ext : (code == 2u ? ext : 0.0f);
 }
 
+// The shift that was added to a raw coordinate to give its staged value.
+__device__ __forceinline__ float staged_shift(float staged, float raw, float ext)
+{
+    const float d = staged - raw;
+    return d > 0.5f * ext ? ext : (d < -0.5f * ext ? -ext : 0.0f);
+}
+
 __device__ __forceinline__ int wrap_index(int v, int m) { return v < 0 ? v + m : (v >= m ? v - m : v); }
 
 // Per-warp staging area, kStage candidates (a multiple of 32) per batch.
 template <int kStage>
 struct WarpSmem {
-    float4 xy[kStage / 2];           // pre-shifted (x_a, x_b, y_a, y_b) of slots 2p, 2p+1
-    float2 zz[kStage / 2];           // pre-shifted (z_a, z_b)
-    float4 raw[kStage];              // unshifted x, y, z; .w = type | shift code << 8
+    float4 xy[kStage / 2];              // staged (x_a, x_b, y_a, y_b) of slots 2p, 2p+1
+    float2 zz[kStage / 2];              // staged (z_a, z_b)
+    uint32_t meta[kStage];              // sorted index | type << 27
     uint32_t mask[(kStage / 32) * 32];  // [group][lane]
 };
 
@@ -76,36 +87,62 @@ struct Lane {
     int count;
 };
 
-template <bool kUniformR>
-__device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float4 o, const float* s_force,
-                                           const float* s_inv_eff, const float* s_thr, const float4* s_shift,
-                                           bool generic)
+struct Tables {
+    const float* force;
+    const float* inv_eff;
+    const float* thr;
+    const float* thr_lo;
+};
+
+// Displacement from the home to a staged candidate: the filter's arithmetic.
+template <bool kGeneric>
+__device__ __forceinline__ void staged_delta(const StepConsts& c, float cx, float cy, float cz, const float4& h,
+                                             float& dx, float& dy, float& dz)
 {
-    float dx = __fsub_rn(o.x, L.h.x);
-    float dy = __fsub_rn(o.y, L.h.y);
-    float dz = __fsub_rn(o.z, L.h.z);
-    const uint32_t wbits = __float_as_uint(o.w);
-    if (generic) {
-        dx = wrap_ref(dx, c.ext[0], c.half[0]);
-        dy = wrap_ref(dy, c.ext[1], c.half[1]);
-        dz = wrap_ref(dz, c.ext[2], c.half[2]);
+    if (kGeneric) {
+        dx = wrap_ref(cx - h.x, c.ext[0], c.half[0]);
+        dy = wrap_ref(cy - h.y, c.ext[1], c.half[1]);
+        dz = wrap_ref(cz - h.z, c.ext[2], c.half[2]);
     } else {
-        const float4 sh = s_shift[(wbits >> 8) & 63u];
-        dx = __fadd_rn(dx, sh.x);
-        dy = __fadd_rn(dy, sh.y);
-        dz = __fadd_rn(dz, sh.z);
+        dx = cx - h.x;
+        dy = cy - h.y;
+        dz = cz - h.z;
     }
-    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-    const float s = __fadd_rn(d2, 0.0001f);
-    const uint32_t pair = L.tp * kTableStride + (wbits & (kTableStride - 1));
-    const float thr = kUniformR ? c.thr_uniform : s_thr[pair];
-    if (s < thr) {
+}
+
+// One queued pair: certain-interaction bound, exact fallback, force term.
+template <bool kGeneric, bool kUniformR>
+__device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float cx, float cy, float cz,
+                                           uint32_t meta, const float4* __restrict__ pos_sorted, const Tables& tb)
+{
+    float dx, dy, dz;
+    staged_delta<kGeneric>(c, cx, cy, cz, L.h, dx, dy, dz);
+    const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const uint32_t pair = L.tp * kTableStride + (meta >> kTypeShift);
+    bool inter = d2 < (kUniformR ? c.thr_lo_uniform : tb.thr_lo[pair]);
+    if (!inter) {
+        // within rounding of the threshold: the reference's exact test
+        const float4 o = pos_sorted[meta & kIndexMask];
+        float ex = __fsub_rn(o.x, L.h.x), ey = __fsub_rn(o.y, L.h.y), ez = __fsub_rn(o.z, L.h.z);
+        if (kGeneric) {
+            ex = wrap_ref(ex, c.ext[0], c.half[0]);
+            ey = wrap_ref(ey, c.ext[1], c.half[1]);
+            ez = wrap_ref(ez, c.ext[2], c.half[2]);
+        } else {
+            ex = __fadd_rn(ex, staged_shift(cx, o.x, c.ext[0]));
+            ey = __fadd_rn(ey, staged_shift(cy, o.y, c.ext[1]));
+            ez = __fadd_rn(ez, staged_shift(cz, o.z, c.ext[2]));
+        }
+        const float e2 = __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
+        inter = __fadd_rn(e2, 0.0001f) < (kUniformR ? c.thr_uniform : tb.thr[pair]);
+    }
+    if (inter) {
         L.count++;
+        const float s = d2 + 0.0001f;
         const float rs = rsqrtf(s);
-        const float dist = s * rs;
-        const float r = dist * (kUniformR ? c.inv_eff_uniform : s_inv_eff[pair]);
+        const float r = s * rs * (kUniformR ? c.inv_eff_uniform : tb.inv_eff[pair]);
         const float ex = __expf(c.neg_k * r * r);
-        const float net = fmaf(c.repulsion, ex, -c.attraction * r) * s_force[pair];
+        const float net = fmaf(c.repulsion, ex, -c.attraction * r) * tb.force[pair];
         const float wgt = net * rs;
         L.fx = fmaf(dx, wgt, L.fx);
         L.fy = fmaf(dy, wgt, L.fy);
@@ -113,8 +150,8 @@ __device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float4 
     }
 }
 
-template <int kStage, bool kGeneric, bool kUniformR>
-__global__ void __launch_bounds__(kThreads)
+template <int kStage, int kMinBlocks, bool kGeneric, bool kUniformR>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
     step_force_kernel(StepConsts c, const PairTables* __restrict__ tables, const float4* __restrict__ pos_sorted,
                       const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ vals_sorted,
                       const uint32_t* __restrict__ cell_off, const int2* __restrict__ items,
@@ -124,7 +161,7 @@ __global__ void __launch_bounds__(kThreads)
     __shared__ float s_force[kTableSize];
     __shared__ float s_inv_eff[kUniformR ? 1 : kTableSize];
     __shared__ float s_thr[kUniformR ? 1 : kTableSize];
-    __shared__ float4 s_shift[64];  // periodic shift of each shift code
+    __shared__ float s_thr_lo[kUniformR ? 1 : kTableSize];
     extern __shared__ __align__(16) unsigned char s_dyn[];
     const int T = c.num_types;
     for (int e = threadIdx.x; e < T * T; e += kThreads) {
@@ -134,19 +171,18 @@ __global__ void __launch_bounds__(kThreads)
         if (!kUniformR) {
             s_inv_eff[k] = 1.0f / tables->eff[k];
             s_thr[k] = tables->threshold[k];
+            s_thr_lo[k] = tables->threshold_lo[k];
         }
     }
-    if (threadIdx.x < 64) {
-        const uint32_t code = threadIdx.x;
-        s_shift[code] = make_float4(code_shift(code & 3u, c.ext[0]), code_shift((code >> 2) & 3u, c.ext[1]),
-                                    code_shift((code >> 4) & 3u, c.ext[2]), 0.0f);
-    }
     __syncthreads();
+    const Tables tb{s_force, s_inv_eff, s_thr, s_thr_lo};
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int item = blockIdx.x * kWarps + warp;
     if (item >= *n_items) return;
     WarpSmem<kStage>& w = reinterpret_cast<WarpSmem<kStage>*>(s_dyn)[warp];
+    const float* xyf = reinterpret_cast<const float*>(w.xy);
+    const float* zzf = reinterpret_cast<const float*>(w.zz);
     const int2 it = items[item];
     const bool active = lane < it.y;
     const int t = it.x + (active ? lane : 0);
@@ -237,14 +273,14 @@ __global__ void __launch_bounds__(kThreads)
                 const float sz = code_shift(code >> 4, c.ext[2]);
                 for (int g = lo + lane; g < hi; g += 32) {
                     const int slot = g - base;
-                    float4 p = pos_sorted[beg + (g - pre)];
+                    const int j = beg + (g - pre);
+                    const float4 p = pos_sorted[j];
                     float* xy = reinterpret_cast<float*>(&w.xy[slot >> 1]);
                     float* zv = reinterpret_cast<float*>(&w.zz[slot >> 1]);
                     xy[slot & 1] = p.x + sx;
                     xy[2 + (slot & 1)] = p.y + sy;
                     zv[slot & 1] = p.z + sz;
-                    p.w = __uint_as_float((__float_as_uint(p.w) & 0xffu) | (code << 8));
-                    w.raw[slot] = p;
+                    w.meta[slot] = (uint32_t)j | ((__float_as_uint(p.w) & (kTableStride - 1)) << kTypeShift);
                 }
             }
             // padding up to a whole group: never passes the filter
@@ -259,15 +295,15 @@ __global__ void __launch_bounds__(kThreads)
 
             // ---- filter: one bit per candidate
             if (kGeneric) {
+                const float4 hh = make_float4(hxf, hyf, hzf, 0.0f);
                 for (int gi = 0; gi < ngroups; gi++) {
                     uint32_t m = 0;
                     for (int q = 0; q < 32; q++) {
                         const int slot = gi * 32 + q;
                         if (slot >= lim) break;
-                        const float4 o = w.raw[slot];
-                        const float dx = wrap_ref(o.x - hxf, c.ext[0], c.half[0]);
-                        const float dy = wrap_ref(o.y - hyf, c.ext[1], c.half[1]);
-                        const float dz = wrap_ref(o.z - hzf, c.ext[2], c.half[2]);
+                        float dx, dy, dz;
+                        staged_delta<true>(c, xyf[(slot >> 1) * 4 + (slot & 1)],
+                                           xyf[(slot >> 1) * 4 + 2 + (slot & 1)], zzf[slot], hh, dx, dy, dz);
                         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                         if (d2 < thr_f) m |= 1u << q;
                     }
@@ -294,9 +330,8 @@ __global__ void __launch_bounds__(kThreads)
                     w.mask[gi * 32 + lane] = m;
                 }
             }
-            __syncwarp();
 
-            // ---- drain: exact test and force for every set bit
+            // ---- drain: every set bit of this lane
             int gi = 0;
             uint32_t m = w.mask[lane];
             while (true) {
@@ -309,8 +344,11 @@ __global__ void __launch_bounds__(kThreads)
                 if (has) {
                     const int slot = gi * 32 + (__ffs(m) - 1);
                     m &= m - 1u;
-                    if (slot != own)
-                        pair_force<kUniformR>(c, L, w.raw[slot], s_force, s_inv_eff, s_thr, s_shift, kGeneric);
+                    if (slot != own) {
+                        const int pb = (slot >> 1) * 4 + (slot & 1);
+                        pair_force<kGeneric, kUniformR>(c, L, xyf[pb], xyf[pb + 2], zzf[slot], w.meta[slot],
+                                                        pos_sorted, tb);
+                    }
                 }
             }
             __syncwarp();
@@ -376,49 +414,35 @@ __global__ void __launch_bounds__(1024)
     if (tid == 1023) *n_items = (int)s_chunk[1023];
 }
 
-}  // namespace
-
-int max_step_items(int n, const Grid& g) { return (n + 31) / 32 + g.m[1] * g.m[2]; }
-
-int step_launches(int n) { return n > 0 ? 2 : 0; }
-
-cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, int2* items, int* n_items,
-                             cudaStream_t st)
+template <int S, int B, bool G, bool U>
+cudaError_t configure_one()
 {
-    if (n <= 0) return cudaMemsetAsync(n_items, 0, sizeof(int), st);
-    plan_kernel<<<1, 1024, 0, st>>>(cell_off, g.m[0], g.m[1] * g.m[2], items, n_items);
-    return cudaGetLastError();
-}
-
-namespace {
-
-template <int S, bool G, bool U>
-cudaError_t configure_variant()
-{
-    return cudaFuncSetAttribute(step_force_kernel<S, G, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(step_force_kernel<S, B, G, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(WarpSmem<S>) * kWarps));
 }
 
-template <int S>
-cudaError_t configure_stage()
+template <int S, int B>
+cudaError_t configure_variant()
 {
-    cudaError_t e = configure_variant<S, false, false>();
-    if (e == cudaSuccess) e = configure_variant<S, false, true>();
-    if (e == cudaSuccess) e = configure_variant<S, true, false>();
-    if (e == cudaSuccess) e = configure_variant<S, true, true>();
+    cudaError_t e = configure_one<S, B, false, false>();
+    if (e == cudaSuccess) e = configure_one<S, B, false, true>();
+    if (e == cudaSuccess) e = configure_one<S, B, true, false>();
+    if (e == cudaSuccess) e = configure_one<S, B, true, true>();
     return e;
 }
 
-template <int S>
-cudaError_t launch_stage(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
-                         const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
-                         const int2* items, const int* n_items, int blocks, float4* pos, float4* vel, float4* acc,
-                         int* counts, cudaStream_t st)
+// Variant S = staged candidates per batch, B = resident blocks per SM the
+// register budget is sized for.
+template <int S, int B>
+cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
+                           const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
+                           const int2* items, const int* n_items, int blocks, float4* pos, float4* vel, float4* acc,
+                           int* counts, cudaStream_t st)
 {
     const size_t smem = sizeof(WarpSmem<S>) * kWarps;
-#define CF_FORCE_LAUNCH(G, U)                                                                                     \
-    step_force_kernel<S, G, U><<<blocks, kThreads, smem, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted,   \
-                                                               cell_off, items, n_items, pos, vel, acc, counts)
+#define CF_FORCE_LAUNCH(G, U)                                                                                        \
+    step_force_kernel<S, B, G, U><<<blocks, kThreads, smem, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted,   \
+                                                                  cell_off, items, n_items, pos, vel, acc, counts)
     if (c.grid.generic) {
         if (c.uniform_r)
             CF_FORCE_LAUNCH(true, true);
@@ -436,12 +460,25 @@ cudaError_t launch_stage(const StepConsts& c, const PairTables* tables, const fl
 
 }  // namespace
 
+int max_step_items(int n, const Grid& g) { return (n + 31) / 32 + g.m[1] * g.m[2]; }
+
+int step_launches(int n) { return n > 0 ? 2 : 0; }
+
+cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, int2* items, int* n_items,
+                             cudaStream_t st)
+{
+    if (n <= 0) return cudaMemsetAsync(n_items, 0, sizeof(int), st);
+    plan_kernel<<<1, 1024, 0, st>>>(cell_off, g.m[0], g.m[1] * g.m[2], items, n_items);
+    return cudaGetLastError();
+}
+
 // Opt the force kernels into their dynamic shared memory (outside any
 // stream capture).
 cudaError_t configure_step_force()
 {
-    cudaError_t e = configure_stage<256>();
-    if (e == cudaSuccess) e = configure_stage<512>();
+    cudaError_t e = configure_variant<256, 8>();
+    if (e == cudaSuccess) e = configure_variant<256, 6>();
+    if (e == cudaSuccess) e = configure_variant<512, 4>();
     return e;
 }
 
@@ -452,11 +489,17 @@ cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, con
 {
     if (c.n <= 0 || max_items <= 0) return cudaSuccess;
     const int blocks = (max_items + kWarps - 1) / kWarps;
-    if (c.stage == 256)
-        return launch_stage<256>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items, blocks,
-                                 pos, vel, acc, counts, st);
-    return launch_stage<512>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items, blocks, pos,
-                             vel, acc, counts, st);
+    switch (c.variant) {
+    case 1:
+        return launch_variant<256, 6>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+                                      blocks, pos, vel, acc, counts, st);
+    case 2:
+        return launch_variant<512, 4>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+                                      blocks, pos, vel, acc, counts, st);
+    default:
+        return launch_variant<256, 8>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+                                      blocks, pos, vel, acc, counts, st);
+    }
 }
 
 }  // namespace cf

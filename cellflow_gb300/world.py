@@ -210,14 +210,14 @@ class ParticleSimulation:
         check(self._lib.cf_step(self._h, C.byref(p), steps), "cf_step")
 
     def autotune(self, params: SimulationParams, steps: int = 3) -> int:
-        """Pick the force kernel's staging batch by timing trial steps; the state is restored."""
+        """Pick the force-kernel variant by timing trial steps; the state is restored."""
         p = params.to_c()
         chosen = C.c_int()
         check(self._lib.cf_autotune_step(self._h, C.byref(p), steps, C.byref(chosen)), "cf_autotune_step")
         return chosen.value
 
-    def set_force_stage(self, stage: int) -> None:
-        check(self._lib.cf_set_force_stage(self._h, stage), "cf_set_force_stage")
+    def set_force_variant(self, variant: int) -> None:
+        check(self._lib.cf_set_force_variant(self._h, variant), "cf_set_force_variant")
 
     def grid(self, params: SimulationParams) -> GridInfo:
         g = GridInfo()

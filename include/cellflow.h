@@ -180,14 +180,17 @@ float cf_lfo_ratio(float ratio, float lfo_a, float lfo_s, float t_seconds);
  * builds the cell list, computes forces, neighbour counts and the
  * density-adaptive scale, integrates and wraps.  Asynchronous. */
 int cf_step(cf_world* w, const cf_step_params* p, int nsteps);
+/* Force-kernel variants: 0 = 256 candidates staged per warp batch, register
+ * budget for 8 blocks per SM; 1 = 256 staged, 6 blocks per SM; 2 = 512
+ * staged, 4 blocks per SM.  Results are bit-identical across variants. */
+#define CF_FORCE_VARIANTS 3
 /* Autotuner of the step (no counterpart in the reference): runs `steps`
- * trial steps with each staging batch size of the force kernel (256 and 512
- * candidates per warp batch), restores the particle state, keeps the faster
- * variant for later steps and returns it in *chosen_stage.  Results are
- * identical whichever variant runs; only speed differs. */
-int cf_autotune_step(cf_world* w, const cf_step_params* p, int steps, int* chosen_stage);
-/* Set the staging batch directly (256 or 512). */
-int cf_set_force_stage(cf_world* w, int stage);
+ * trial steps with each force-kernel variant, restores the particle state,
+ * keeps the fastest variant for later steps and returns it in
+ * *chosen_variant. */
+int cf_autotune_step(cf_world* w, const cf_step_params* p, int steps, int* chosen_variant);
+/* Select a force-kernel variant directly. */
+int cf_set_force_variant(cf_world* w, int variant);
 /* The grid cf_step would use for these parameters. */
 int cf_get_grid(cf_world* w, const cf_step_params* p, cf_grid_info* out);
 /* Build the cell list of the current positions with the step's grid and

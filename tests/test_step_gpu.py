@@ -160,26 +160,27 @@ def test_rollout_short(cflib):
 
 
 def test_autotune_keeps_state_and_results(cflib):
-    """Both staging variants give bit-identical steps; autotuning restores the state."""
+    """All force-kernel variants give bit-identical steps; autotuning restores the state."""
     w = inputs.Workload("tune", n=30000, num_types=5, radius=0.12, steps=1, seed=19)
     params = w.params()
     sim, pos, types, table, radio = make_world(w)
     before = sim.get_state()
-    stage = sim.autotune(params, 2)
-    assert stage in (256, 512)
+    chosen = sim.autotune(params, 2)
+    assert chosen in (0, 1, 2)
     after = sim.get_state()
     for a, b in zip(before, after):
         assert np.array_equal(a, b)
-    sim.simulate(params, 2)
-    ref = sim.getParticleData()
-    sim2, *_ = make_world(w, pos, types, table, radio)
-    sim2.set_force_stage(512 if stage == 256 else 256)
-    sim2.simulate(params, 2)
-    rec2 = sim2.getParticleData()
     sim.close()
-    sim2.close()
-    for f in ("pos", "vel", "acc"):
-        assert np.array_equal(ref[f], rec2[f]), f
+    results = []
+    for variant in range(3):
+        s, *_ = make_world(w, pos, types, table, radio)
+        s.set_force_variant(variant)
+        s.simulate(params, 2)
+        results.append(s.getParticleData())
+        s.close()
+    for rec in results[1:]:
+        for f in ("pos", "vel", "acc"):
+            assert np.array_equal(results[0][f], rec[f]), f
 
 
 def test_zero_table_is_pure_friction(cflib):
