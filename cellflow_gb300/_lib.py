@@ -157,6 +157,20 @@ _SIGNATURES = {
         [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p, C.c_int,
          _P(C.c_int), C.c_void_p],
     ),
+    "cf_batch_create": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_uint64,
+                                  _P(_W)]),
+    "cf_batch_destroy": (C.c_int, [_W]),
+    "cf_batch_info": (C.c_int, [_W, _P(C.c_int), _P(C.c_int), C.c_void_p]),
+    "cf_batch_world": (C.c_int, [_W, _P(_W)]),
+    "cf_batch_set_state": (C.c_int, [_W, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cf_batch_get_state": (C.c_int, [_W, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cf_batch_set_force_tables": (C.c_int, [_W, C.c_void_p, C.c_int]),
+    "cf_batch_step": (C.c_int, [_W, _P(StepParams), C.c_int]),
+    "cf_batch_capture": (C.c_int, [_W, _P(StepParams), C.c_int]),
+    "cf_batch_replay": (C.c_int, [_W]),
+    "cf_batch_autotune": (C.c_int, [_W, _P(StepParams), C.c_int, _P(C.c_int)]),
+    "cf_batch_sync": (C.c_int, [_W]),
+    "cf_batch_set_stream": (C.c_int, [_W, C.c_void_p]),
     "cf_profile_enable": (C.c_int, [_W, C.c_int]),
     "cf_profile_read": (C.c_int, [_W, _P(PhaseTimes)]),
     "cf_measure_fp32_peak": (C.c_int, [_P(C.c_double)]),

@@ -61,8 +61,13 @@ void dev_free(void* p)
     if (p) cudaFree(p);
 }
 
+void apply_worlds(Grid& g, int worlds);
+
 void drop_graphs(cf_world* w)
 {
+    if (w->batch_graph) cudaGraphExecDestroy(w->batch_graph);
+    w->batch_graph = nullptr;
+    w->batch_graph_steps = 0;
     for (int k = 0; k < 2; k++) {
         if (w->graph[k]) cudaGraphExecDestroy(w->graph[k]);
         w->graph[k] = nullptr;
@@ -352,6 +357,9 @@ int prepare_step(cf_world* w, const cf_step_params* p, StepConsts* c)
     c->variant = w->force_variant;
     c->thr_filter = filter_bound(thr_max, std::max(c->ext[0], std::max(c->ext[1], c->ext[2])));
     c->grid = choose_step_grid(c->ext, r_cut, kMaxCells);
+    apply_worlds(c->grid, w->worlds);
+    // force tables: one per world (a plain world uses the pair tables' own)
+    c->world_force = w->worlds > 1 ? w->world_tables : w->tables->force;
     c->n = w->n;
     c->num_types = w->num_types;
     c->repulsion = p->repulsion;
@@ -363,6 +371,16 @@ int prepare_step(cf_world* w, const cf_step_params* p, StepConsts* c)
     c->friction = p->friction;
     c->max_expected_neighbors = p->max_expected_neighbors;
     return CF_OK;
+}
+
+// Extend a per-world grid to a batch of worlds sharing its shape.
+void apply_worlds(Grid& g, int worlds)
+{
+    g.worlds = worlds;
+    g.cells_w = g.m[0] * g.m[1] * g.m[2];
+    g.cells = worlds * g.cells_w;
+    g.key_bits = 0;
+    while ((1ll << g.key_bits) < (long long)g.cells) g.key_bits++;
 }
 
 // One step's launches on the world's stream: cell list, then the fused force,
@@ -522,6 +540,8 @@ void finish_grid(Grid& g, const float* ext, int max_cells)
     }
     for (int a = 0; a < 3; a++) g.inv[a] = (float)((double)g.m[a] / (double)ext[a]);
     g.cells = g.m[0] * g.m[1] * g.m[2];
+    g.worlds = 1;
+    g.cells_w = g.cells;
     g.key_bits = 0;
     while ((1ll << g.key_bits) < (long long)g.cells) g.key_bits++;
 }
@@ -568,6 +588,8 @@ Grid canonical_grid(const float* ext, float r_max)
     }
     for (int a = 0; a < 3; a++) g.inv[a] = (float)((double)g.m[a] / (double)ext[a]);
     g.cells = g.m[0] * g.m[1] * g.m[2];
+    g.worlds = 1;
+    g.cells_w = g.cells;
     return g;
 }
 
@@ -658,6 +680,7 @@ int cf_destroy(cf_world* w)
     free_particles(w);
     dev_free(w->err);
     dev_free(w->tables);
+    dev_free(w->world_tables);
     if (w->own_stream) cudaStreamDestroy(w->own_stream);
     delete w;
     return CF_OK;
@@ -1147,6 +1170,7 @@ int cf_work_counters(cf_world* w, const cf_step_params* p, uint64_t* c27, uint64
     for (int a = 0; a < w->num_types; a++)
         for (int b = 0; b < w->num_types; b++) r_max = std::max(r_max, w->host_tables.eff[a * kTableStride + b]);
     Grid g = canonical_grid(c.ext, r_max);
+    apply_worlds(g, w->worlds);
     Scratch& s = w->s;
     if ((size_t)g.cells > s.pop_cap) {
         CF_CUDA(cudaStreamSynchronize(w->stream));
@@ -1244,6 +1268,240 @@ int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, cons
     }
     if (2 * (size_t)total > (size_t)cap_vertices) return fail(CF_ERR_CAPACITY, "vertex buffer too small");
     return CF_OK;
+}
+
+}  // extern "C"
+
+// ---- batched ensembles ------------------------------------------------------
+//
+// A batch is one cf_world whose particles belong to several independent
+// worlds: world k owns particles [off[k], off[k+1]), carries its index in the
+// bits of pos4.w above the type, and has its own force table.  Cell ids are
+// world * cells_per_world + cell, so one cell list, one plan and one force
+// launch per step cover every world; no pair ever crosses worlds.
+
+struct cf_batch {
+    cf_world* w = nullptr;
+};
+
+namespace {
+
+int check_batch(const cf_batch* b)
+{
+    if (!b || !b->w) return fail(CF_ERR_INVALID, "null batch");
+    return CF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cf_batch_create(int worlds, const int* n_per_world, int num_types, float w_, float h_, float d_, uint64_t seed,
+                    cf_batch** out)
+{
+    if (!out) return fail(CF_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (worlds < 1 || worlds > (1 << 20) || !n_per_world) return fail(CF_ERR_INVALID, "worlds must be in [1, 2^20]");
+    long long total = 0;
+    for (int k = 0; k < worlds; k++) {
+        if (n_per_world[k] < 0) return fail(CF_ERR_INVALID, "particle counts must be >= 0");
+        total += n_per_world[k];
+    }
+    if (total > (1ll << 27) - 1) return fail(CF_ERR_INVALID, "a batch holds at most 2^27 - 1 particles");
+    cf_world* w = nullptr;
+    int rc = cf_create((int)total, num_types, w_, h_, d_, seed, &w);
+    if (rc) return rc;
+    w->worlds = worlds;
+    w->world_off.assign(worlds + 1, 0);
+    for (int k = 0; k < worlds; k++) w->world_off[k + 1] = w->world_off[k] + n_per_world[k];
+    cudaError_t e = dev_alloc(&w->world_tables, (size_t)worlds * kTableSize);
+    if (e != cudaSuccess) {
+        cf_destroy(w);
+        return cuda_fail(e, "cudaMalloc(world tables)");
+    }
+    // world k: particles spawned from seed + k, raw table from seed + k, the
+    // default transform (ParticleSimulation.cu:513-519)
+    std::vector<float> tables((size_t)worlds * kTableSize, 0.0f);
+    float lo[3], span[3];
+    for (int a = 0; a < 3; a++) {
+        span[a] = std::min(2000.0f, w->ext[a]);
+        lo[a] = (w->ext[a] - span[a]) * 0.5f;
+    }
+    for (int k = 0; k < worlds && e == cudaSuccess; k++) {
+        const int off = w->world_off[k], n = n_per_world[k];
+        e = launch_init_particles(w->pos + off, w->vel + off, w->acc + off, w->counts + off, n, num_types, lo, span,
+                                  seed + (uint64_t)k, w->stream, (uint32_t)k);
+        uint64_t s = (seed + (uint64_t)k) ^ 0x2545F4914F6CDD1Dull;
+        for (int a = 0; a < num_types; a++)
+            for (int b2 = 0; b2 < num_types; b2++) {
+                const float raw = uniform_pm1(s);
+                const float t = tanhf(raw * 1.0f) * 0.28f + -0.20f;
+                tables[(size_t)k * kTableSize + a * kTableStride + b2] = fmaxf(-1.0f, fminf(1.0f, t));
+            }
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(w->world_tables, tables.data(), sizeof(float) * tables.size(), cudaMemcpyHostToDevice,
+                            w->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
+    if (e != cudaSuccess) {
+        cf_destroy(w);
+        return cuda_fail(e, "cf_batch_create");
+    }
+    cf_batch* b = new cf_batch();
+    b->w = w;
+    *out = b;
+    return CF_OK;
+}
+
+int cf_batch_destroy(cf_batch* b)
+{
+    if (!b) return CF_OK;
+    cf_destroy(b->w);
+    delete b;
+    return CF_OK;
+}
+
+int cf_batch_world(cf_batch* b, cf_world** out)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    if (!out) return fail(CF_ERR_INVALID, "null output");
+    *out = b->w;
+    return CF_OK;
+}
+
+int cf_batch_info(const cf_batch* b, int* worlds, int* total, int* offsets)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    if (worlds) *worlds = b->w->worlds;
+    if (total) *total = b->w->n;
+    if (offsets) std::memcpy(offsets, b->w->world_off.data(), sizeof(int) * (b->w->worlds + 1));
+    return CF_OK;
+}
+
+int cf_batch_set_state(cf_batch* b, const float* pos4, const float* vel4, const int* counts)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    cf_world* w = b->w;
+    std::vector<float> tagged;
+    if (pos4) {
+        // add each particle's world index above its type bits
+        tagged.assign(pos4, pos4 + 4 * (size_t)w->n);
+        for (int k = 0; k < w->worlds; k++)
+            for (int i = w->world_off[k]; i < w->world_off[k + 1]; i++) {
+                uint32_t bits;
+                std::memcpy(&bits, &tagged[4 * (size_t)i + 3], 4);
+                bits = (bits & kTypeMask) | ((uint32_t)k << kWorldShift);
+                std::memcpy(&tagged[4 * (size_t)i + 3], &bits, 4);
+            }
+    }
+    return cf_set_state(w, pos4 ? tagged.data() : nullptr, vel4, counts);
+}
+
+int cf_batch_get_state(cf_batch* b, float* pos4, float* vel4, int* counts)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    rc = cf_get_state(b->w, pos4, vel4, counts);
+    if (rc || !pos4) return rc;
+    for (size_t i = 0; i < (size_t)b->w->n; i++) {
+        uint32_t bits;
+        std::memcpy(&bits, &pos4[4 * i + 3], 4);
+        bits &= kTypeMask;
+        std::memcpy(&pos4[4 * i + 3], &bits, 4);
+    }
+    return CF_OK;
+}
+
+int cf_batch_set_force_tables(cf_batch* b, const float* tables, int count)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    cf_world* w = b->w;
+    const int T = w->num_types;
+    if (!tables || count != w->worlds * T * T) return fail(CF_ERR_INVALID, "count must be worlds * T * T");
+    std::vector<float> padded((size_t)w->worlds * kTableSize, 0.0f);
+    for (int k = 0; k < w->worlds; k++)
+        for (int a = 0; a < T; a++)
+            for (int c = 0; c < T; c++)
+                padded[(size_t)k * kTableSize + a * kTableStride + c] = tables[((size_t)k * T + a) * T + c];
+    CF_CUDA(cudaMemcpyAsync(w->world_tables, padded.data(), sizeof(float) * padded.size(), cudaMemcpyHostToDevice,
+                            w->stream));
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    return CF_OK;
+}
+
+int cf_batch_step(cf_batch* b, const cf_step_params* p, int nsteps)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    return cf_step(b->w, p, nsteps);
+}
+
+int cf_batch_capture(cf_batch* b, const cf_step_params* p, int nsteps)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    cf_world* w = b->w;
+    if (nsteps < 1) return fail(CF_ERR_INVALID, "nsteps must be >= 1");
+    if (!w->stream) return fail(CF_ERR_INVALID, "capture needs a non-default stream");
+    StepConsts c;
+    rc = prepare_step(w, p, &c);
+    if (rc) return rc;
+    rc = ensure_cells(w, c.grid.cells);
+    if (!rc) rc = ensure_plan(w, c.grid);
+    if (!rc) rc = ensure_offsets(w, c.grid.cells);
+    if (rc) return rc;
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    if (w->batch_graph) cudaGraphExecDestroy(w->batch_graph);
+    w->batch_graph = nullptr;
+    w->batch_graph_steps = 0;
+    cudaGraph_t graph = nullptr;
+    CF_CUDA(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < nsteps && rc == CF_OK; s++) rc = enqueue_step(w, c, 0);
+    cudaError_t e = cudaStreamEndCapture(w->stream, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&w->batch_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    w->batch_graph_steps = nsteps;
+    return CF_OK;
+}
+
+int cf_batch_replay(cf_batch* b)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    if (!b->w->batch_graph) return fail(CF_ERR_INVALID, "no captured graph (cf_batch_capture)");
+    CF_CUDA(cudaGraphLaunch(b->w->batch_graph, b->w->stream));
+    return CF_OK;
+}
+
+int cf_batch_autotune(cf_batch* b, const cf_step_params* p, int steps, int* chosen_variant)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    return cf_autotune_step(b->w, p, steps, chosen_variant);
+}
+
+int cf_batch_sync(cf_batch* b)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    return cf_sync(b->w);
+}
+
+int cf_batch_set_stream(cf_batch* b, void* stream)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    return cf_set_stream(b->w, stream);
 }
 
 }  // extern "C"

@@ -42,8 +42,9 @@ __global__ void __launch_bounds__(kThreads)
     keys[i] = (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
 }
 
-// Cell id of every particle and the population of every cell (counts must be
-// zero on entry); flags positions and types like cell_hash_kernel.
+// Cell id of every particle (world * cells_w + cell) and the population of
+// every cell (counts must be zero on entry); flags positions outside the box,
+// types outside [0, T) and world indices outside the batch.
 __global__ void __launch_bounds__(kThreads)
     cell_hash_count_kernel(const float4* __restrict__ pos, int n, Grid g, float ex, float ey, float ez, int num_types,
                            uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, int* __restrict__ err)
@@ -53,11 +54,14 @@ __global__ void __launch_bounds__(kThreads)
     float4 p = pos[i];
     bool inside = (p.x >= 0.0f && p.x < ex) && (p.y >= 0.0f && p.y < ey) && (p.z >= 0.0f && p.z < ez);
     if (!inside) atomicOr(err, kDevErrDomain);
-    if (__float_as_uint(p.w) >= (uint32_t)num_types) atomicOr(err, kDevErrType);
+    const uint32_t bits = __float_as_uint(p.w);
+    uint32_t world = bits >> kWorldShift;
+    if ((bits & kTypeMask) >= (uint32_t)num_types || world >= (uint32_t)g.worlds) atomicOr(err, kDevErrType);
+    if (world >= (uint32_t)g.worlds) world = 0;
     int cx = cell_coord(p.x, g.inv[0], g.m[0]);
     int cy = cell_coord(p.y, g.inv[1], g.m[1]);
     int cz = cell_coord(p.z, g.inv[2], g.m[2]);
-    const uint32_t key = (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
+    const uint32_t key = world * (uint32_t)g.cells_w + (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
     keys[i] = key;
     atomicAdd(&counts[key], 1u);
 }
@@ -243,12 +247,15 @@ __global__ void __launch_bounds__(kThreads)
 
 // ---- work counters ---------------------------------------------------------
 
+// Cell of a particle in the work-model grid of its own world (world-major).
 __device__ __forceinline__ uint32_t canon_cell(float4 p, const Grid& g)
 {
     int cx = cell_coord(p.x, g.inv[0], g.m[0]);
     int cy = cell_coord(p.y, g.inv[1], g.m[1]);
     int cz = cell_coord(p.z, g.inv[2], g.m[2]);
-    return (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
+    uint32_t world = __float_as_uint(p.w) >> kWorldShift;
+    if (world >= (uint32_t)g.worlds) world = 0;
+    return world * (uint32_t)g.cells_w + (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -279,7 +286,10 @@ __global__ void __launch_bounds__(kThreads)
     int i = blockIdx.x * kThreads + threadIdx.x;
     unsigned long long cand = 0, inter = 0;
     if (i < n) {
-        uint32_t c = canon_cell(pos[i], g);
+        const uint32_t key = canon_cell(pos[i], g);
+        const uint32_t world = key / (uint32_t)g.cells_w;
+        const uint32_t c = key - world * (uint32_t)g.cells_w;
+        const uint32_t base = world * (uint32_t)g.cells_w;
         int cx = (int)(c % (uint32_t)g.m[0]);
         int cy = (int)((c / (uint32_t)g.m[0]) % (uint32_t)g.m[1]);
         int cz = (int)(c / (uint32_t)(g.m[0] * g.m[1]));
@@ -287,7 +297,7 @@ __global__ void __launch_bounds__(kThreads)
         int nx = stencil_axis(cx, g.m[0], ox), ny = stencil_axis(cy, g.m[1], oy), nz = stencil_axis(cz, g.m[2], oz);
         for (int a = 0; a < nz; a++)
             for (int b = 0; b < ny; b++)
-                for (int e = 0; e < nx; e++) cand += pop[(oz[a] * g.m[1] + oy[b]) * g.m[0] + ox[e]];
+                for (int e = 0; e < nx; e++) cand += pop[base + (oz[a] * g.m[1] + oy[b]) * g.m[0] + ox[e]];
         cand -= 1;
         inter = (unsigned long long)counts[i];
     }

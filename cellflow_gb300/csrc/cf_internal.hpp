@@ -41,15 +41,22 @@ struct PairTables {
     float threshold_lo[kTableSize];  // contracted d^2 below this interacts for certain
 };
 
-// Grid of one cell list.
+// Grid of one cell list.  A batch of independent worlds shares one grid
+// shape; a cell id is world * cells_w + (z * m1 + y) * m0 + x.
 struct Grid {
     int m[3];         // cells per axis
     float inv[3];     // hash multipliers, float(m / extent)
-    int cells;        // m0 * m1 * m2
+    int cells;        // total cells: worlds * cells_w
     int key_bits;     // bits of a cell id
     int generic;      // 1: full reference wrap per candidate (some axis < 5 cells)
     int periodic;     // 1: periodic stencil (step), 0: clipped (proximity)
+    int worlds;       // independent worlds sharing the grid (1 for a plain world)
+    int cells_w;      // cells per world: m0 * m1 * m2
 };
+
+// pos4.w of a particle: type in the low 5 bits, world index above.
+constexpr int kWorldShift = 5;
+constexpr uint32_t kTypeMask = (1u << kWorldShift) - 1u;
 
 // Everything the step kernels read besides the buffers.
 struct StepConsts {
@@ -67,6 +74,7 @@ struct StepConsts {
     int variant;       // force-kernel variant (staging batch, occupancy), see cf_set_force_variant
     float repulsion, attraction, neg_k, balance, force_multiplier, delta_t, friction;
     int max_expected_neighbors;
+    const float* world_force;  // per-world force tables, kTableSize floats each (32-stride)
 };
 
 struct Scratch {
@@ -106,6 +114,11 @@ struct cf_world {
     int n = 0;
     int num_types = 0;
     float ext[3] = {0, 0, 0};
+    // a batch of independent worlds (cf_batch_*): world k owns particles
+    // [world_off[k], world_off[k + 1]) and force table world_tables[k]
+    int worlds = 1;
+    std::vector<int> world_off;
+    float* world_tables = nullptr;  // device, worlds * kTableSize floats (32-stride)
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     float4* pos = nullptr;
@@ -140,6 +153,9 @@ struct cf_world {
     const void* graph_bufs[2] = {nullptr, nullptr};
     bool use_graphs = true;
     int force_variant = 0;  // force-kernel variant, chosen by cf_autotune_step
+    // a captured multi-step graph (cf_batch_capture) and the constants it was captured with
+    cudaGraphExec_t batch_graph = nullptr;
+    int batch_graph_steps = 0;
 };
 
 namespace cf {
@@ -187,7 +203,8 @@ cudaError_t launch_proximity_emit_vertices(const int32_t* slots, const uint32_t*
                                            const float4* pos, const float* colors, int n_colors, float* vertices,
                                            int cap_vertices, cudaStream_t st);
 cudaError_t launch_init_particles(float4* pos, float4* vel, float4* acc, int* counts, int n, int num_types,
-                                  const float* lo, const float* span, uint64_t seed, cudaStream_t st);
+                                  const float* lo, const float* span, uint64_t seed, cudaStream_t st,
+                                  uint32_t world = 0);
 cudaError_t launch_aos_to_soa(const cf_particle* aos, float4* pos, float4* vel, float4* acc, int n, cudaStream_t st);
 cudaError_t launch_soa_to_aos(const float4* pos, const float4* vel, const float4* acc, cf_particle* aos, int n,
                               cudaStream_t st);

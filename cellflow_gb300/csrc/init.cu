@@ -38,7 +38,7 @@ __device__ __forceinline__ float unit24(uint32_t v) { return (float)(v >> 8) * (
 __global__ void __launch_bounds__(kThreads)
     init_particles_kernel(float4* __restrict__ pos, float4* __restrict__ vel, float4* __restrict__ acc,
                           int* __restrict__ counts, int n, int num_types, float lo_x, float lo_y, float lo_z,
-                          float span_x, float span_y, float span_z, uint2 key)
+                          float span_x, float span_y, float span_z, uint2 key, uint32_t world)
 {
     const int i = blockIdx.x * kThreads + threadIdx.x;
     if (i >= n) return;
@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kThreads)
     const float y = __fadd_rn(lo_y, __fmul_rn(unit24(r.y), span_y));
     const float z = __fadd_rn(lo_z, __fmul_rn(unit24(r.z), span_z));
     const uint32_t type = (uint32_t)(((unsigned long long)r.w * (unsigned long long)num_types) >> 32);
-    pos[i] = make_float4(x, y, z, __uint_as_float(type));
+    pos[i] = make_float4(x, y, z, __uint_as_float(type | (world << kWorldShift)));
     vel[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     acc[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     counts[i] = 0;
@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(kThreads)
     o.acc[0] = a.x;
     o.acc[1] = a.y;
     o.acc[2] = a.z;
-    o.ptype = __float_as_uint(p.w);
+    o.ptype = __float_as_uint(p.w) & kTypeMask;  // world bits stay internal
     o.pad = 0.0f;
     aos[i] = o;
 }
@@ -90,12 +90,12 @@ __global__ void __launch_bounds__(kThreads)
 }  // namespace
 
 cudaError_t launch_init_particles(float4* pos, float4* vel, float4* acc, int* counts, int n, int num_types,
-                                  const float* lo, const float* span, uint64_t seed, cudaStream_t st)
+                                  const float* lo, const float* span, uint64_t seed, cudaStream_t st, uint32_t world)
 {
     if (n <= 0) return cudaSuccess;
     const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
     init_particles_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
-        pos, vel, acc, counts, n, num_types, lo[0], lo[1], lo[2], span[0], span[1], span[2], key);
+        pos, vel, acc, counts, n, num_types, lo[0], lo[1], lo[2], span[0], span[1], span[2], key, world);
     return cudaGetLastError();
 }
 

@@ -88,10 +88,11 @@ struct Lane {
 };
 
 struct Tables {
-    const float* force;
+    const float* force;  // the item's world, T-stride
     const float* inv_eff;
     const float* thr;
     const float* thr_lo;
+    int T;
 };
 
 // Displacement from the home to a staged candidate: the filter's arithmetic.
@@ -118,7 +119,8 @@ __device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float c
     float dx, dy, dz;
     staged_delta<kGeneric>(c, cx, cy, cz, L.h, dx, dy, dz);
     const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    const uint32_t pair = L.tp * kTableStride + (meta >> kTypeShift);
+    const uint32_t other = meta >> kTypeShift;
+    const uint32_t pair = L.tp * kTableStride + other;
     bool inter = d2 < (kUniformR ? c.thr_lo_uniform : tb.thr_lo[pair]);
     if (!inter) {
         // within rounding of the threshold: the reference's exact test
@@ -142,7 +144,7 @@ __device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float c
         const float rs = rsqrtf(s);
         const float r = s * rs * (kUniformR ? c.inv_eff_uniform : tb.inv_eff[pair]);
         const float ex = __expf(c.neg_k * r * r);
-        const float net = fmaf(c.repulsion, ex, -c.attraction * r) * tb.force[pair];
+        const float net = fmaf(c.repulsion, ex, -c.attraction * r) * tb.force[L.tp * tb.T + other];
         const float wgt = net * rs;
         L.fx = fmaf(dx, wgt, L.fx);
         L.fy = fmaf(dy, wgt, L.fy);
@@ -158,29 +160,27 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                       const int* __restrict__ n_items, float4* __restrict__ pos, float4* __restrict__ vel,
                       float4* __restrict__ acc, int* __restrict__ counts)
 {
-    __shared__ float s_force[kTableSize];
     __shared__ float s_inv_eff[kUniformR ? 1 : kTableSize];
     __shared__ float s_thr[kUniformR ? 1 : kTableSize];
     __shared__ float s_thr_lo[kUniformR ? 1 : kTableSize];
     extern __shared__ __align__(16) unsigned char s_dyn[];
     const int T = c.num_types;
-    for (int e = threadIdx.x; e < T * T; e += kThreads) {
-        const int a = e / T, b = e - a * T;
-        const int k = a * kTableStride + b;
-        s_force[k] = tables->force[k];
-        if (!kUniformR) {
+    if (!kUniformR) {
+        for (int e = threadIdx.x; e < T * T; e += kThreads) {
+            const int a = e / T, b = e - a * T;
+            const int k = a * kTableStride + b;
             s_inv_eff[k] = 1.0f / tables->eff[k];
             s_thr[k] = tables->threshold[k];
             s_thr_lo[k] = tables->threshold_lo[k];
         }
     }
     __syncthreads();
-    const Tables tb{s_force, s_inv_eff, s_thr, s_thr_lo};
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int item = blockIdx.x * kWarps + warp;
     if (item >= *n_items) return;
     WarpSmem<kStage>& w = reinterpret_cast<WarpSmem<kStage>*>(s_dyn)[warp];
+    float* wforce = reinterpret_cast<float*>(s_dyn + sizeof(WarpSmem<kStage>) * kWarps) + warp * T * T;
     const float* xyf = reinterpret_cast<const float*>(w.xy);
     const float* zzf = reinterpret_cast<const float*>(w.zz);
     const int2 it = items[item];
@@ -188,17 +188,29 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const int t = it.x + (active ? lane : 0);
     Lane L;
     L.h = pos_sorted[t];
-    L.tp = __float_as_uint(L.h.w) & (kTableStride - 1);
+    L.tp = __float_as_uint(L.h.w) & kTypeMask;
     L.fx = L.fy = L.fz = 0.0f;
     L.count = 0;
 
+    // cell coordinates inside the item's world (items never straddle worlds)
     const int mx = c.grid.m[0], my = c.grid.m[1], mz = c.grid.m[2];
+    const uint32_t cells_w = (uint32_t)c.grid.cells_w;
     const uint32_t key_first = keys_sorted[it.x];
-    const int x0 = (int)(key_first % (uint32_t)mx);
-    const int x1 = (int)(keys_sorted[it.x + it.y - 1] % (uint32_t)mx);
-    const int yc = (int)((key_first / (uint32_t)mx) % (uint32_t)my);
-    const int zc = (int)(key_first / (uint32_t)(mx * my));
-    const int hx = (int)(keys_sorted[t] % (uint32_t)mx);
+    const uint32_t world = key_first / cells_w;
+    const uint32_t world_base = world * cells_w;
+    const uint32_t local_first = key_first - world_base;
+    const int x0 = (int)(local_first % (uint32_t)mx);
+    const int x1 = (int)((keys_sorted[it.x + it.y - 1] - world_base) % (uint32_t)mx);
+    const int yc = (int)((local_first / (uint32_t)mx) % (uint32_t)my);
+    const int zc = (int)(local_first / (uint32_t)(mx * my));
+    const int hx = (int)((keys_sorted[t] - world_base) % (uint32_t)mx);
+    // the world's force table, compact T-stride
+    for (int e = lane; e < T * T; e += 32) {
+        const int a = e / T, b = e - a * T;
+        wforce[e] = c.world_force[(size_t)world * kTableSize + a * kTableStride + b];
+    }
+    __syncwarp();
+    const Tables tb{wforce, s_inv_eff, s_thr, s_thr_lo, T};
     // x sub-ranges whose union (range plus one cell each side) fits in the box
     const int width = kGeneric ? mx : (mx - 2);
     const int passes = kGeneric ? 1 : (x1 - x0 + width) / width;
@@ -237,7 +249,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 b = a - 1;
             }
             if (row < ny * nz && b >= a) {
-                const uint32_t base = (uint32_t)((zz * my + yy) * mx);
+                const uint32_t base = world_base + (uint32_t)((zz * my + yy) * mx);
                 seg_beg = (int)cell_off[base + a];
                 seg_len = (int)cell_off[base + b + 1] - seg_beg;
                 seg_code = kGeneric ? 0u : (cx | (cy << 2) | (cz << 4));
@@ -418,7 +430,7 @@ template <int S, int B, bool G, bool U>
 cudaError_t configure_one()
 {
     return cudaFuncSetAttribute(step_force_kernel<S, B, G, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(sizeof(WarpSmem<S>) * kWarps));
+                                (int)((sizeof(WarpSmem<S>) + sizeof(float) * kTableSize) * kWarps));
 }
 
 template <int S, int B>
@@ -439,7 +451,7 @@ cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const 
                            const int2* items, const int* n_items, int blocks, float4* pos, float4* vel, float4* acc,
                            int* counts, cudaStream_t st)
 {
-    const size_t smem = sizeof(WarpSmem<S>) * kWarps;
+    const size_t smem = (sizeof(WarpSmem<S>) + sizeof(float) * c.num_types * c.num_types) * kWarps;
 #define CF_FORCE_LAUNCH(G, U)                                                                                        \
     step_force_kernel<S, B, G, U><<<blocks, kThreads, smem, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted,   \
                                                                   cell_off, items, n_items, pos, vel, acc, counts)
@@ -460,7 +472,7 @@ cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const 
 
 }  // namespace
 
-int max_step_items(int n, const Grid& g) { return (n + 31) / 32 + g.m[1] * g.m[2]; }
+int max_step_items(int n, const Grid& g) { return (n + 31) / 32 + g.worlds * g.m[1] * g.m[2]; }
 
 int step_launches(int n) { return n > 0 ? 2 : 0; }
 
@@ -468,7 +480,7 @@ cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, int
                              cudaStream_t st)
 {
     if (n <= 0) return cudaMemsetAsync(n_items, 0, sizeof(int), st);
-    plan_kernel<<<1, 1024, 0, st>>>(cell_off, g.m[0], g.m[1] * g.m[2], items, n_items);
+    plan_kernel<<<1, 1024, 0, st>>>(cell_off, g.m[0], g.worlds * g.m[1] * g.m[2], items, n_items);
     return cudaGetLastError();
 }
 

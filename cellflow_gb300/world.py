@@ -266,6 +266,90 @@ class ParticleSimulation:
         return count.value
 
 
+class Batch:
+    """Many independent worlds stepped together (cf_batch_*): world k owns particles
+    offsets[k]:offsets[k+1] of the concatenated state and has its own force table."""
+
+    def __init__(self, n_per_world, num_types: int, width: float = 2.0, height: float = 2.0, depth: float = 2.0,
+                 seed: int = 1):
+        lib = load()
+        self._lib = lib
+        self._h = C.c_void_p()
+        counts = np.ascontiguousarray(n_per_world, dtype=np.int32)
+        check(lib.cf_batch_create(len(counts), _ptr(counts), num_types, width, height, depth, seed,
+                                  C.byref(self._h)), "cf_batch_create")
+        worlds, total = C.c_int(), C.c_int()
+        check(lib.cf_batch_info(self._h, C.byref(worlds), C.byref(total), None), "cf_batch_info")
+        self.offsets = np.zeros(worlds.value + 1, dtype=np.int32)
+        check(lib.cf_batch_info(self._h, None, None, _ptr(self.offsets)), "cf_batch_info")
+        self.n = total.value
+        self.num_types = num_types
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.cf_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def world_handle(self) -> C.c_void_p:
+        out = C.c_void_p()
+        check(self._lib.cf_batch_world(self._h, C.byref(out)), "cf_batch_world")
+        return out
+
+    def set_particles(self, pos: np.ndarray, types: np.ndarray, vel: np.ndarray | None = None) -> None:
+        pos4 = np.zeros((self.n, 4), dtype=np.float32)
+        pos4[:, :3] = pos
+        pos4[:, 3] = np.asarray(types, dtype=np.uint32).view(np.float32)
+        vel4 = np.zeros((self.n, 4), dtype=np.float32)
+        if vel is not None:
+            vel4[:, :3] = vel
+        counts = np.zeros(self.n, dtype=np.int32)
+        check(self._lib.cf_batch_set_state(self._h, _ptr(pos4), _ptr(vel4), _ptr(counts)), "cf_batch_set_state")
+
+    def get_state(self):
+        pos4 = np.zeros((self.n, 4), dtype=np.float32)
+        vel4 = np.zeros((self.n, 4), dtype=np.float32)
+        counts = np.zeros(self.n, dtype=np.int32)
+        check(self._lib.cf_batch_get_state(self._h, _ptr(pos4), _ptr(vel4), _ptr(counts)), "cf_batch_get_state")
+        return pos4, vel4, counts
+
+    def set_force_tables(self, tables) -> None:
+        t = np.ascontiguousarray(tables, dtype=np.float32).ravel()
+        check(self._lib.cf_batch_set_force_tables(self._h, _ptr(t), t.size), "cf_batch_set_force_tables")
+
+    def simulate(self, params: SimulationParams, steps: int = 1) -> None:
+        p = params.to_c()
+        check(self._lib.cf_batch_step(self._h, C.byref(p), steps), "cf_batch_step")
+
+    def capture(self, params: SimulationParams, steps: int) -> None:
+        p = params.to_c()
+        check(self._lib.cf_batch_capture(self._h, C.byref(p), steps), "cf_batch_capture")
+
+    def replay(self) -> None:
+        check(self._lib.cf_batch_replay(self._h), "cf_batch_replay")
+
+    def autotune(self, params: SimulationParams, steps: int = 2) -> int:
+        p = params.to_c()
+        chosen = C.c_int()
+        check(self._lib.cf_batch_autotune(self._h, C.byref(p), steps, C.byref(chosen)), "cf_batch_autotune")
+        return chosen.value
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(self._lib.cf_batch_set_stream(self._h, C.c_void_p(stream_ptr or 0)), "cf_batch_set_stream")
+
+    def sync(self) -> None:
+        check(self._lib.cf_batch_sync(self._h), "cf_batch_sync")
+
+
 def lfo_ratio(ratio: float, lfo_a: float, lfo_s: float, t: float) -> float:
     """Caller LFO of CellFlowWidget::paintGL (CellFlowWidget.cpp:414-421)."""
     return load().cf_lfo_ratio(ratio, lfo_a, lfo_s, t)

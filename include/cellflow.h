@@ -246,6 +246,40 @@ int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, cons
 int cf_proximity_edges_noalloc(const void* d_pos4, int n, float width, float height, float depth, float distance,
                                int max_conn, int32_t* d_edges, int cap, int* n_edges, void* stream);
 
+/* ---- batched ensembles (no counterpart in the reference) ------------------ */
+
+/* Many independent worlds of uneven size, each with its own force table,
+ * sharing the step parameters and box; one cell list, one plan and one force
+ * launch per step cover all of them.  World k owns particles
+ * [offsets[k], offsets[k+1]) of the concatenated state.  A batch of one world
+ * steps exactly like cf_step; every world of a batch steps exactly like the
+ * same world run alone (bit for bit). */
+typedef struct cf_batch cf_batch;
+
+/* Worlds spawned as cf_initialize_particles(seed + k, 2000) and given the
+ * default force table of a raw table drawn from seed + k. */
+int cf_batch_create(int worlds, const int* n_per_world, int num_types, float w, float h, float d, uint64_t seed,
+                    cf_batch** out);
+int cf_batch_destroy(cf_batch* b);
+/* worlds, total particles, offsets[worlds + 1] (any may be NULL). */
+int cf_batch_info(const cf_batch* b, int* worlds, int* total, int* offsets);
+/* The batch as one cf_world (profiling, work counters, device buffers); its
+ * pos4.w carries the world index above the type bits. */
+int cf_batch_world(cf_batch* b, cf_world** out);
+/* Concatenated SoA state; pos4.w = type (the world index is implied by the
+ * offsets). */
+int cf_batch_set_state(cf_batch* b, const float* pos4, const float* vel4, const int* counts);
+int cf_batch_get_state(cf_batch* b, float* pos4, float* vel4, int* counts);
+/* worlds * T * T values, world-major, each row-major [self*T + other]. */
+int cf_batch_set_force_tables(cf_batch* b, const float* tables, int count);
+int cf_batch_step(cf_batch* b, const cf_step_params* p, int nsteps);
+/* Capture nsteps steps into one CUDA graph; cf_batch_replay launches it. */
+int cf_batch_capture(cf_batch* b, const cf_step_params* p, int nsteps);
+int cf_batch_replay(cf_batch* b);
+int cf_batch_autotune(cf_batch* b, const cf_step_params* p, int steps, int* chosen_variant);
+int cf_batch_sync(cf_batch* b);
+int cf_batch_set_stream(cf_batch* b, void* cuda_stream);
+
 /* ---- measurement ---------------------------------------------------------- */
 
 /* Device time of the step's phases, accumulated over the steps run since
