@@ -159,10 +159,6 @@ def run_reference_arm(args, rank, world):
 
     from cellflow_gb300 import inputs
 
-    w = inputs.WORKLOADS[args.workload]
-    params = w.params()
-    pos, types, table = w.positions(), w.types(), w.table()
-    radio = np.zeros(w.num_types, np.float32)
     import oracle
 
     try:
@@ -171,39 +167,71 @@ def run_reference_arm(args, rank, world):
         pass
     kind = "reference" if oracle.ref_available() else "port"
     cores = os.cpu_count() or 1
-    vel = np.zeros_like(pos)
-    counts = np.zeros(w.n, np.int32)
-    rec = oracle.to_records(pos, vel, types)
-    # each step: a strided sample of rows sized to about one second
-    stride = max(1, w.n // (8 * cores))
 
-    def one(stride_):
-        rows = (0, w.n, stride_)
+    if args.workload in inputs.BATCHED:
+        # the reference steps one world at a time: step s samples world (37 s) mod worlds
+        bw = inputs.BATCHED[args.workload]
+        params = bw.params()
+        sizes = bw.sizes()
+        total_n = int(sizes.sum())
+        config = {"workload": bw.name, "worlds": bw.worlds, "total_particles": total_n, "types": bw.num_types,
+                  "radius": bw.radius, "seed": bw.seed}
+        worlds_in = {}
+
+        def world_inputs(s):
+            k = (37 * s) % bw.worlds
+            if k not in worlds_in:
+                p, t, tab = bw.world(k, int(sizes[k]))
+                worlds_in[k] = (p, t, tab, oracle.to_records(p, np.zeros_like(p), t))
+            return worlds_in[k]
+        radio = np.zeros(bw.num_types, np.float32)
+        full_n = total_n
+    else:
+        w = inputs.WORKLOADS[args.workload]
+        params = w.params()
+        p0, t0_, tab0 = w.positions(), w.types(), w.table()
+        fixed = (p0, t0_, tab0, oracle.to_records(p0, np.zeros_like(p0), t0_))
+        config = workload_config(w)
+
+        def world_inputs(s):
+            return fixed
+        radio = np.zeros(w.num_types, np.float32)
+        full_n = w.n
+
+    # each step: a strided sample of rows of one world, sized to about one second
+    def one(s, frac):
+        pos, types, table, rec = world_inputs(s)
+        n = len(pos)
+        stride_ = max(1, int(round(1.0 / frac)))
+        rows = (0, n, stride_)
+        counts = np.zeros(n, np.int32)
         t0 = time.perf_counter()
         if kind == "reference":
             oracle.ref_step(rec, table, radio, counts, params, rows=rows)
         else:
-            oracle.step_f32(pos, vel, types, counts, table, radio, params, rows=rows)
-        return time.perf_counter() - t0, len(range(*rows))
+            oracle.step_f32(pos, np.zeros_like(pos), types, counts, table, radio, params, rows=rows)
+        return time.perf_counter() - t0, len(range(*rows)), n
 
-    dt, r = one(stride)
-    stride = max(1, int(stride * dt / 1.0)) if dt > 0 else stride
-    for _ in range(args.warmup):
-        one(stride)
+    frac = min(1.0, 8.0 * cores / max(len(world_inputs(0)[0]), 1))
+    dt, r, _ = one(0, frac)
+    if dt > 0:
+        frac = min(1.0, frac / dt)
+    for s in range(args.warmup):
+        one(s, frac)
     total_t, total_rows = 0.0, 0
-    for _ in range(args.steps):
-        dt, r = one(stride)
+    for s in range(args.steps):
+        dt, r, _ = one(s, frac)
         total_t += dt
         total_rows += r
     value = total_rows / total_t
-    sample = (f"per step {total_rows // max(args.steps, 1)} of {w.n} particles (every {stride}th), each against "
-              f"all {w.n}; {cores} OpenMP threads")
+    sample = (f"per step about {total_rows // max(args.steps, 1)} particles (a {frac:.3g} strided fraction of one "
+              f"world), each against all particles of its world; {cores} OpenMP threads")
     line = {
         "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * w.n / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": 1e3 * full_n / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded Philox), see config",
-        "config": workload_config(w),
+        "config": config,
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": kind,
                          "sample": sample},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -375,6 +403,152 @@ def run_gb300(args, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
+def run_batched(args, rank, world, local):
+    """--workload batched_256w: 256 independent worlds stepped together (cf_batch_*), a
+    100-step loop captured in one CUDA graph and replayed; the same worlds stepped one by
+    one through the plain API (each world's step its own CUDA graph) are timed beside it.
+    One bench step is one simulation step of every world; K is rounded up to whole
+    replays of the 100-step graph."""
+    import numpy as np
+    import torch
+
+    import cellflow_gb300 as cf
+    from cellflow_gb300 import _lib, inputs
+    from cellflow_gb300.world import Batch, ParticleSimulation
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    bw = inputs.BATCHED[args.workload]
+    params = bw.params()
+    sizes = bw.sizes()
+    parts = [bw.world(k, int(n)) for k, n in enumerate(sizes)]
+    pos = np.concatenate([p[0] for p in parts])
+    types = np.concatenate([p[1] for p in parts])
+    tables = np.stack([p[2] for p in parts])
+    total = int(sizes.sum())
+    stream = torch.cuda.Stream()
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    batch = Batch(sizes, bw.num_types, bw.extent, bw.extent, bw.extent, seed=bw.seed)
+    batch.set_stream(stream.cuda_stream)
+    batch.set_particles(pos, types)
+    batch.set_force_tables(tables)
+    variant = batch.autotune(params, 3)
+    batch.capture(params, bw.graph_steps)
+    _, graph_kernels = batch.graph_info()
+    replays = max(1, -(-args.steps // bw.graph_steps))
+    warm = max(1, -(-args.warmup // bw.graph_steps))
+    for _ in range(warm):
+        batch.replay()
+    batch.sync()
+    batch.set_particles(pos, types)  # timed replays start from the initial state
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(replays)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    with torch.cuda.stream(stream):
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(stream)
+            batch.replay()
+            e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    batch_ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
+    t_max = batch_ms
+    if world > 1:
+        t = torch.tensor([batch_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    steps_timed = replays * bw.graph_steps
+    value = total * steps_timed * world / (t_max * 1e-3)
+
+    # ---- end to end: host state in (pinned), one replay, host state out
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt).pin_memory()  # noqa: E731
+    hpos, hvel, hcnt = pin((total, 4), torch.float32), pin((total, 4), torch.float32), pin((total,), torch.int32)
+    batch.set_particles(pos, types)
+    lib = _lib.load()
+    ptrs = [C.c_void_p(x.data_ptr()) for x in (hpos, hvel, hcnt)]
+    _lib.check(lib.cf_batch_get_state(batch.handle, *ptrs), "cf_batch_get_state")
+    e2e_reps = max(1, replays)
+    barrier()
+    e2e_wall = 0.0
+    for _ in range(e2e_reps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _lib.check(lib.cf_batch_set_state(batch.handle, *ptrs), "cf_batch_set_state")
+        batch.replay()
+        _lib.check(lib.cf_batch_get_state(batch.handle, *ptrs), "cf_batch_get_state")
+        e2e_wall += time.perf_counter() - t0
+    e2e_value = total * bw.graph_steps * e2e_reps * world / e2e_wall
+    batch.close()
+
+    # ---- the same worlds stepped one by one through the plain step, same stream
+    sims = []
+    for k, n in enumerate(sizes):
+        s = ParticleSimulation(int(n), bw.num_types, bw.extent, bw.extent, bw.extent)
+        s.set_stream(stream.cuda_stream)
+        s.set_particles(parts[k][0], parts[k][1])
+        s.setForceTable(parts[k][2])
+        s.setRadioByType(np.zeros(bw.num_types, np.float32))
+        s.set_force_variant(variant)
+        sims.append(s)
+    for s in sims:
+        s.simulate(params, 2)
+    torch.cuda.synchronize()
+    for k, s in enumerate(sims):
+        s.set_particles(parts[k][0], parts[k][1])
+    wbw_steps = bw.graph_steps
+    with torch.cuda.stream(stream):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for s in sims:
+            s.simulate(params, wbw_steps)
+        e1.record(stream)
+    e1.synchronize()
+    wbw_ms = e0.elapsed_time(e1)
+    wbw_value = total * wbw_steps / (wbw_ms * 1e-3)
+    for s in sims:
+        s.close()
+
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": steps_timed, "warmup": warm * bw.graph_steps, "ms_per_step": t_max / steps_timed,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Philox4x32-10): per world uniform positions, uniform types, N(0,0.5) table",
+            "config": {"workload": bw.name, "worlds": bw.worlds, "n_per_world": f"log-uniform [{bw.n_min}, "
+                       f"{bw.n_max}]", "total_particles": total, "n_min": int(sizes.min()),
+                       "n_max": int(sizes.max()), "types": bw.num_types, "radius": bw.radius, "dt": bw.delta_t,
+                       "graph_steps": bw.graph_steps, "replays": replays, "force_variant": variant,
+                       "l2": "flushed between replays (256 MiB write); state larger than L2", "seed": bw.seed},
+            "world_by_world": {"value": wbw_value, "unit": "particle-steps/s", "steps": wbw_steps,
+                               "path": "256 ParticleSimulation objects on one stream, one step graph each"},
+            "batched_over_world_by_world": value / wbw_value,
+            "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": total * 36 //
+                    bw.graph_steps, "d2h_bytes_per_step": total * 36 // bw.graph_steps,
+                    "path": "cf_batch_set_state (pinned) + 100-step graph replay + cf_batch_get_state",
+                    "replays": e2e_reps},
+            "gpu_launches": graph_kernels * replays,
+            "clocks": clk,
+            "library": cf.__name__ + ": " + lib.cf_version().decode(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def reference_gpu_kernel(w, params, pos, types, table, radio, stream):
     """The reference step kernel (sm_103a build of ParticleSimulation.cu:69-166) on the same
     inputs, launched as ParticleSimulation::simulate does; a few steps, CUDA events."""
@@ -425,6 +599,11 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
+        return
+    from cellflow_gb300 import inputs
+
+    if args.workload in inputs.BATCHED:
+        run_batched(args, rank, world, local)
         return
     run_gb300(args, rank, world, local)
 

@@ -168,6 +168,7 @@ _SIGNATURES = {
     "cf_batch_step": (C.c_int, [_W, _P(StepParams), C.c_int]),
     "cf_batch_capture": (C.c_int, [_W, _P(StepParams), C.c_int]),
     "cf_batch_replay": (C.c_int, [_W]),
+    "cf_batch_graph_info": (C.c_int, [_W, _P(C.c_int), _P(C.c_longlong)]),
     "cf_batch_autotune": (C.c_int, [_W, _P(StepParams), C.c_int, _P(C.c_int)]),
     "cf_batch_sync": (C.c_int, [_W]),
     "cf_batch_set_stream": (C.c_int, [_W, C.c_void_p]),

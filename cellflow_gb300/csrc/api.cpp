@@ -1467,10 +1467,36 @@ int cf_batch_capture(cf_batch* b, const cf_step_params* p, int nsteps)
         return rc;
     }
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    size_t nodes = 0;
+    long long kernels = 0;
+    e = cudaGraphGetNodes(graph, nullptr, &nodes);
+    if (e == cudaSuccess && nodes) {
+        std::vector<cudaGraphNode_t> list(nodes);
+        e = cudaGraphGetNodes(graph, list.data(), &nodes);
+        for (size_t i = 0; i < nodes && e == cudaSuccess; i++) {
+            cudaGraphNodeType t;
+            e = cudaGraphNodeGetType(list[i], &t);
+            if (e == cudaSuccess && t == cudaGraphNodeTypeKernel) kernels++;
+        }
+    }
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return cuda_fail(e, "cudaGraphGetNodes");
+    }
     e = cudaGraphInstantiate(&w->batch_graph, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
     w->batch_graph_steps = nsteps;
+    w->batch_graph_kernels = kernels;
+    return CF_OK;
+}
+
+int cf_batch_graph_info(const cf_batch* b, int* steps, long long* kernels)
+{
+    int rc = check_batch(b);
+    if (rc) return rc;
+    if (steps) *steps = b->w->batch_graph_steps;
+    if (kernels) *kernels = b->w->batch_graph_kernels;
     return CF_OK;
 }
 

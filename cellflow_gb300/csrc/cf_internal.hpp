@@ -156,6 +156,7 @@ struct cf_world {
     // a captured multi-step graph (cf_batch_capture) and the constants it was captured with
     cudaGraphExec_t batch_graph = nullptr;
     int batch_graph_steps = 0;
+    long long batch_graph_kernels = 0;  // kernel nodes of the captured graph
 };
 
 namespace cf {

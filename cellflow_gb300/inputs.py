@@ -139,6 +139,38 @@ class Workload:
         return gaussian_table(self.num_types, self.table_mean, self.table_sigma, self.seed)
 
 
+@dataclass
+class BatchedWorkload:
+    """Independent worlds of log-uniform size, each with its own seeded inputs."""
+
+    name: str
+    worlds: int
+    n_min: int
+    n_max: int
+    num_types: int
+    radius: float
+    graph_steps: int
+    seed: int
+    table_sigma: float = 0.5
+    extent: float = 2.0
+    delta_t: float = 0.01
+
+    def sizes(self) -> np.ndarray:
+        u = unit24(_words(self.worlds, 7, self.seed)).astype(np.float64)
+        lo, hi = np.log(self.n_min), np.log(self.n_max)
+        return np.rint(np.exp(lo + u * (hi - lo))).astype(np.int32)
+
+    def world(self, k: int, n: int):
+        """Positions, types and force table of world k (seeded seed + k)."""
+        s = self.seed + k
+        return uniform_positions(n, s), uniform_types(n, self.num_types, s), gaussian_table(
+            self.num_types, 0.0, self.table_sigma, s)
+
+    def params(self):
+        return Workload(self.name, n=1, num_types=self.num_types, radius=self.radius, steps=self.graph_steps,
+                        extent=self.extent, delta_t=self.delta_t).params()
+
+
 # The configurations of the benchmark suite (W = H = D = 2 after the shift).
 PLAIN_SMALL = Workload("plain_n4096_t6", n=4096, num_types=6, radius=0.1, steps=100, seed=0x5EED0001)
 README_SCALE = Workload("plain_n100k_t8", n=100_000, num_types=8, radius=0.0920, steps=1000, seed=0x5EED0002,
@@ -146,3 +178,6 @@ README_SCALE = Workload("plain_n100k_t8", n=100_000, num_types=8, radius=0.0920,
 BLOBS_1M = Workload("blobs_n1m_t12", n=1_000_000, num_types=12, radius=0.02, steps=500, table_mean=0.1,
                     table_sigma=0.6, blobs=64, blob_sigma=0.02, seed=0x5EED0003)
 WORKLOADS = {w.name: w for w in (PLAIN_SMALL, README_SCALE, BLOBS_1M)}
+BATCHED_256 = BatchedWorkload("batched_256w", worlds=256, n_min=2048, n_max=65536, num_types=6, radius=0.1,
+                              graph_steps=100, seed=0x5EED0004)
+BATCHED = {BATCHED_256.name: BATCHED_256}

@@ -337,6 +337,12 @@ class Batch:
     def replay(self) -> None:
         check(self._lib.cf_batch_replay(self._h), "cf_batch_replay")
 
+    def graph_info(self) -> tuple[int, int]:
+        """(steps, kernel nodes) of the captured graph."""
+        steps, kernels = C.c_int(), C.c_longlong()
+        check(self._lib.cf_batch_graph_info(self._h, C.byref(steps), C.byref(kernels)), "cf_batch_graph_info")
+        return steps.value, kernels.value
+
     def autotune(self, params: SimulationParams, steps: int = 2) -> int:
         p = params.to_c()
         chosen = C.c_int()

@@ -276,6 +276,8 @@ int cf_batch_step(cf_batch* b, const cf_step_params* p, int nsteps);
 /* Capture nsteps steps into one CUDA graph; cf_batch_replay launches it. */
 int cf_batch_capture(cf_batch* b, const cf_step_params* p, int nsteps);
 int cf_batch_replay(cf_batch* b);
+/* Steps and kernel nodes of the captured graph (0 and 0 before any capture). */
+int cf_batch_graph_info(const cf_batch* b, int* steps, long long* kernels);
 int cf_batch_autotune(cf_batch* b, const cf_step_params* p, int steps, int* chosen_variant);
 int cf_batch_sync(cf_batch* b);
 int cf_batch_set_stream(cf_batch* b, void* cuda_stream);
