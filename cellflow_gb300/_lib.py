@@ -21,6 +21,8 @@ CF_ERR_DEVICE = -5
 CF_ERR_CAPACITY = -6
 CF_MAX_TYPES = 32
 CF_MAX_PROX_CONN = 16
+# Order of the parameter gradients of cf_rollout_backward (CF_GRAD_*).
+GRAD_PARAMS = ("repulsion", "attraction", "k", "force_multiplier", "balance", "friction")
 
 _ERR_NAMES = {
     CF_ERR_INVALID: "CF_ERR_INVALID",
@@ -172,6 +174,12 @@ _SIGNATURES = {
     "cf_batch_autotune": (C.c_int, [_W, _P(StepParams), C.c_int, _P(C.c_int)]),
     "cf_batch_sync": (C.c_int, [_W]),
     "cf_batch_set_stream": (C.c_int, [_W, C.c_void_p]),
+    "cf_rollout_forward": (C.c_int, [_W, _P(StepParams), C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                     C.c_void_p]),
+    "cf_rollout_backward": (C.c_int, [_W, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                      C.c_void_p]),
+    "cf_rdf": (C.c_int, [_W, C.c_void_p, C.c_int, C.c_float, C.c_void_p]),
+    "cf_rdf_backward": (C.c_int, [_W, C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_void_p]),
     "cf_profile_enable": (C.c_int, [_W, C.c_int]),
     "cf_profile_read": (C.c_int, [_W, _P(PhaseTimes)]),
     "cf_measure_fp32_peak": (C.c_int, [_P(C.c_double)]),

@@ -68,6 +68,8 @@ void drop_graphs(cf_world* w)
     if (w->batch_graph) cudaGraphExecDestroy(w->batch_graph);
     w->batch_graph = nullptr;
     w->batch_graph_steps = 0;
+    if (w->ro.bwd_graph) cudaGraphExecDestroy(w->ro.bwd_graph);
+    w->ro.bwd_graph = nullptr;
     for (int k = 0; k < 2; k++) {
         if (w->graph[k]) cudaGraphExecDestroy(w->graph[k]);
         w->graph[k] = nullptr;
@@ -99,9 +101,22 @@ int alloc_particles(cf_world* w)
     return CF_OK;
 }
 
+void free_rollout(cf_world* w)
+{
+    Rollout& r = w->ro;
+    if (r.bwd_graph) cudaGraphExecDestroy(r.bwd_graph);
+    for (void* p : {(void*)r.ckpt_pos, (void*)r.ckpt_vel, (void*)r.ckpt_cnt, (void*)r.seg_pos, (void*)r.seg_vel,
+                    (void*)r.seg_cnt, (void*)r.fin_pos, (void*)r.fin_vel, (void*)r.fin_cnt, (void*)r.gx,
+                    (void*)r.gv, (void*)r.gf_sorted, (void*)r.ga_sorted, (void*)r.gacc, (void*)r.rdf_pos,
+                    (void*)r.rdf_acc, (void*)r.type_count})
+        dev_free(p);
+    r = Rollout();
+}
+
 void free_particles(cf_world* w)
 {
     drop_graphs(w);
+    free_rollout(w);
     Scratch& s = w->s;
     dev_free(w->pos);
     dev_free(w->vel);
@@ -1528,6 +1543,300 @@ int cf_batch_set_stream(cf_batch* b, void* stream)
     int rc = check_batch(b);
     if (rc) return rc;
     return cf_set_stream(b->w, stream);
+}
+
+}  // extern "C"
+
+// ---- differentiable rollout ---------------------------------------------------
+
+namespace cf {
+namespace {
+
+int ensure_rollout(cf_world* w, int ckpts, int seg_states)
+{
+    Rollout& r = w->ro;
+    const int n = w->n;
+    if (r.n_cap == n && r.gx && ckpts <= r.ckpt_cap && seg_states <= r.seg_cap) return CF_OK;
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    const Rollout keep = r;  // the record of the last forward survives a reallocation
+    free_rollout(w);
+    r.steps = 0;
+    const size_t nn = (size_t)std::max(n, 1);
+    const size_t ck = (size_t)std::max(ckpts, keep.n_cap == n ? keep.ckpt_cap : 0);
+    const size_t sg = (size_t)std::max(seg_states, keep.n_cap == n ? keep.seg_cap : 0);
+    CF_CUDA(dev_alloc(&r.ckpt_pos, nn * ck));
+    CF_CUDA(dev_alloc(&r.ckpt_vel, nn * ck));
+    CF_CUDA(dev_alloc(&r.ckpt_cnt, nn * ck));
+    CF_CUDA(dev_alloc(&r.seg_pos, nn * sg));
+    CF_CUDA(dev_alloc(&r.seg_vel, nn * sg));
+    CF_CUDA(dev_alloc(&r.seg_cnt, nn * sg));
+    CF_CUDA(dev_alloc(&r.fin_pos, nn));
+    CF_CUDA(dev_alloc(&r.fin_vel, nn));
+    CF_CUDA(dev_alloc(&r.fin_cnt, nn));
+    CF_CUDA(dev_alloc(&r.gx, nn));
+    CF_CUDA(dev_alloc(&r.gv, nn));
+    CF_CUDA(dev_alloc(&r.gf_sorted, nn));
+    CF_CUDA(dev_alloc(&r.ga_sorted, nn));
+    CF_CUDA(dev_alloc(&r.gacc, (size_t)kGradAccEntries));
+    r.n_cap = n;
+    r.ckpt_cap = (int)ck;
+    r.seg_cap = (int)sg;
+    return CF_OK;
+}
+
+// Radial distribution scratch (freed with the rest of the rollout buffers
+// whenever the particle count changes).
+int ensure_rdf(cf_world* w)
+{
+    Rollout& r = w->ro;
+    if (r.rdf_pos) return CF_OK;
+    CF_CUDA(dev_alloc(&r.rdf_pos, (size_t)std::max(w->n, 1)));
+    CF_CUDA(dev_alloc(&r.rdf_acc, (size_t)kRdfMaxEntries));
+    CF_CUDA(dev_alloc(&r.type_count, (size_t)CF_MAX_TYPES));
+    return CF_OK;
+}
+
+// Copy a state (positions, velocities, counts) between device buffers.
+int copy_state(cf_world* w, float4* dp, float4* dv, int* dc, const float4* sp, const float4* sv, const int* sc)
+{
+    const size_t n = (size_t)w->n;
+    CF_CUDA(cudaMemcpyAsync(dp, sp, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
+    CF_CUDA(cudaMemcpyAsync(dv, sv, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
+    CF_CUDA(cudaMemcpyAsync(dc, sc, sizeof(int) * n, cudaMemcpyDeviceToDevice, w->stream));
+    return CF_OK;
+}
+
+// The whole backward on the world's stream: save the final state, then per
+// segment (last first) replay the forward from its checkpoint keeping every
+// state, and run the adjoint steps of the segment in reverse; restore the
+// final state.  gx / gv hold dL/dx_K and dL/dv_K on entry, dL/dx_0 and
+// dL/dv_0 on exit; gacc collects the parameter gradients.
+int enqueue_rollout_backward(cf_world* w, const StepConsts& c)
+{
+    Rollout& r = w->ro;
+    const size_t n = (size_t)w->n;
+    int rc = copy_state(w, r.fin_pos, r.fin_vel, r.fin_cnt, w->pos, w->vel, w->counts);
+    if (rc) return rc;
+    CF_CUDA(cudaMemsetAsync(r.gacc, 0, sizeof(double) * kGradAccEntries, w->stream));
+    const int segs = (r.steps + r.every - 1) / r.every;
+    Scratch& s = w->s;
+    for (int seg = segs - 1; seg >= 0; seg--) {
+        const int s0 = seg * r.every;
+        const int len = std::min(r.every, r.steps - s0);
+        rc = copy_state(w, w->pos, w->vel, w->counts, r.ckpt_pos + n * seg, r.ckpt_vel + n * seg,
+                        r.ckpt_cnt + n * seg);
+        if (rc) return rc;
+        for (int t = 0; t < len; t++) {
+            rc = copy_state(w, r.seg_pos + n * t, r.seg_vel + n * t, r.seg_cnt + n * t, w->pos, w->vel, w->counts);
+            if (!rc) rc = enqueue_step(w, c, 0);
+            if (rc) return rc;
+        }
+        CF_CUDA(cudaMemcpyAsync(r.seg_cnt + n * len, w->counts, sizeof(int) * n, cudaMemcpyDeviceToDevice,
+                                w->stream));
+        for (int t = len - 1; t >= 0; t--) {
+            int which = 0;
+            CF_CUDA(launch_cell_list_csr(r.seg_pos + n * t, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, w->err,
+                                         &which, w->stream));
+            CF_CUDA(launch_adjoint_step(c, w->tables, s.pos_sorted, s.keys[which], s.vals[which], s.cell_off,
+                                        r.seg_vel + n * t, r.seg_cnt + n * t, r.seg_cnt + n * (t + 1), r.gx, r.gv,
+                                        r.gf_sorted, r.ga_sorted, r.gacc, w->stream));
+        }
+    }
+    return copy_state(w, w->pos, w->vel, w->counts, r.fin_pos, r.fin_vel, r.fin_cnt);
+}
+
+}  // namespace
+}  // namespace cf
+
+extern "C" {
+
+int cf_rollout_forward(cf_world* w, const cf_step_params* p, const float* d_pos4_in, const float* d_vel4_in,
+                       int nsteps, int checkpoint_every, float* d_pos4_out, float* d_vel4_out)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (w->worlds > 1) return fail(CF_ERR_INVALID, "a rollout runs on a single world");
+    if (nsteps < 1) return fail(CF_ERR_INVALID, "nsteps must be >= 1");
+    if (checkpoint_every < 1) return fail(CF_ERR_INVALID, "checkpoint_every must be >= 1");
+    StepConsts c;
+    rc = prepare_step(w, p, &c);
+    if (!rc) rc = ensure_cells(w, c.grid.cells);
+    if (!rc) rc = ensure_plan(w, c.grid);
+    if (!rc) rc = ensure_offsets(w, c.grid.cells);
+    if (rc) return rc;
+    const int ckpts = (nsteps + checkpoint_every - 1) / checkpoint_every;
+    rc = ensure_rollout(w, ckpts, std::min(checkpoint_every, nsteps) + 1);
+    if (rc) return rc;
+    Rollout& r = w->ro;
+    r.steps = 0;
+    const size_t n = (size_t)w->n;
+    if (d_pos4_in) CF_CUDA(launch_pack_pos(reinterpret_cast<const float4*>(d_pos4_in), w->pos, w->pos, w->n, w->stream));
+    if (d_vel4_in)
+        CF_CUDA(cudaMemcpyAsync(w->vel, d_vel4_in, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
+    cudaGraphExec_t exec = nullptr;
+    if (w->use_graphs && w->stream != nullptr) {
+        rc = step_graph(w, c, 0, &exec);
+        if (rc) return rc;
+    }
+    for (int s = 0; s < nsteps; s++) {
+        if (s % checkpoint_every == 0) {
+            const int k = s / checkpoint_every;
+            rc = copy_state(w, r.ckpt_pos + n * k, r.ckpt_vel + n * k, r.ckpt_cnt + n * k, w->pos, w->vel, w->counts);
+            if (rc) return rc;
+        }
+        if (exec)
+            CF_CUDA(cudaGraphLaunch(exec, w->stream));
+        else if ((rc = enqueue_step(w, c, 0)))
+            return rc;
+    }
+    if (d_pos4_out)
+        CF_CUDA(cudaMemcpyAsync(d_pos4_out, w->pos, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
+    if (d_vel4_out)
+        CF_CUDA(cudaMemcpyAsync(d_vel4_out, w->vel, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
+    r.steps = nsteps;
+    r.every = checkpoint_every;
+    r.n = w->n;
+    r.params = *p;
+    r.table_version = w->table_version;
+    std::memcpy(r.radio, w->radio, sizeof(r.radio));
+    return CF_OK;
+}
+
+int cf_rollout_backward(cf_world* w, const float* d_gpos4, const float* d_gvel4, float* d_gpos4_out,
+                        float* d_gvel4_out, float* grad_force, int grad_force_count, float* grad_params)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    Rollout& r = w->ro;
+    if (r.steps < 1) return fail(CF_ERR_INVALID, "no rollout to differentiate (cf_rollout_forward)");
+    if (r.n != w->n || r.table_version != w->table_version || std::memcmp(r.radio, w->radio, sizeof(r.radio)) != 0)
+        return fail(CF_ERR_INVALID, "the particle count, force table or radii changed since cf_rollout_forward");
+    const int T = w->num_types;
+    if (grad_force && grad_force_count != T * T) return fail(CF_ERR_INVALID, "grad_force_count must be T * T");
+    StepConsts c;
+    rc = prepare_step(w, &r.params, &c);
+    if (!rc) rc = ensure_cells(w, c.grid.cells);
+    if (!rc) rc = ensure_plan(w, c.grid);
+    if (!rc) rc = ensure_offsets(w, c.grid.cells);
+    if (rc) return rc;
+    const size_t n = (size_t)w->n;
+    if (d_gpos4)
+        CF_CUDA(cudaMemcpyAsync(r.gx, d_gpos4, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
+    else
+        CF_CUDA(cudaMemsetAsync(r.gx, 0, sizeof(float4) * n, w->stream));
+    if (d_gvel4)
+        CF_CUDA(cudaMemcpyAsync(r.gv, d_gvel4, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
+    else
+        CF_CUDA(cudaMemsetAsync(r.gv, 0, sizeof(float4) * n, w->stream));
+    if (w->use_graphs && w->stream != nullptr) {
+        const void* bufs = w->s.cell_start;
+        const bool same = r.bwd_graph && r.bwd_steps == r.steps && r.bwd_every == r.every && r.bwd_bufs == bufs &&
+                          std::memcmp(&r.bwd_key, &c, sizeof(c)) == 0;
+        if (!same) {
+            if (r.bwd_graph) cudaGraphExecDestroy(r.bwd_graph);
+            r.bwd_graph = nullptr;
+            cudaGraph_t graph = nullptr;
+            CF_CUDA(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+            rc = enqueue_rollout_backward(w, c);
+            cudaError_t e = cudaStreamEndCapture(w->stream, &graph);
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&r.bwd_graph, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+            r.bwd_key = c;
+            r.bwd_steps = r.steps;
+            r.bwd_every = r.every;
+            r.bwd_bufs = bufs;
+        }
+        CF_CUDA(cudaGraphLaunch(r.bwd_graph, w->stream));
+    } else {
+        rc = enqueue_rollout_backward(w, c);
+        if (rc) return rc;
+    }
+    if (d_gpos4_out)
+        CF_CUDA(cudaMemcpyAsync(d_gpos4_out, r.gx, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
+    if (d_gvel4_out)
+        CF_CUDA(cudaMemcpyAsync(d_gvel4_out, r.gv, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
+    if (grad_force || grad_params) {
+        std::vector<double> acc(kGradAccEntries);
+        CF_CUDA(cudaMemcpyAsync(acc.data(), r.gacc, sizeof(double) * kGradAccEntries, cudaMemcpyDeviceToHost,
+                                w->stream));
+        rc = sync_and_check(w);
+        if (rc) return rc;
+        if (grad_force)
+            for (int a = 0; a < T; a++)
+                for (int b = 0; b < T; b++) grad_force[a * T + b] = (float)acc[a * kTableStride + b];
+        if (grad_params)
+            for (int g = 0; g < CF_GRAD_PARAMS; g++) grad_params[g] = (float)acc[kTableSize + g];
+        return CF_OK;
+    }
+    return CF_OK;
+}
+
+int cf_rdf(cf_world* w, const float* d_pos4, int bins, float r_max, float* d_hist)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (w->worlds > 1) return fail(CF_ERR_INVALID, "the radial distribution covers a single world");
+    const int T = w->num_types;
+    if (bins < 1 || !d_hist || (long long)T * T * bins > kRdfMaxEntries)
+        return fail(CF_ERR_INVALID, "bins must be >= 1 with T * T * bins <= 49152, d_hist not NULL");
+    if (!(r_max > 0.0f) || !std::isfinite(r_max)) return fail(CF_ERR_INVALID, "r_max must be finite and positive");
+    rc = ensure_rdf(w);
+    if (rc) return rc;
+    Grid g = choose_step_grid(w->ext, rdf_cutoff(bins, r_max), kMaxCells);
+    apply_worlds(g, 1);
+    rc = ensure_cells(w, g.cells);
+    if (!rc) rc = ensure_offsets(w, g.cells);
+    if (rc) return rc;
+    CF_CUDA(configure_adjoint());
+    Rollout& r = w->ro;
+    const float4* pos = w->pos;
+    if (d_pos4) {
+        CF_CUDA(launch_pack_pos(reinterpret_cast<const float4*>(d_pos4), w->pos, r.rdf_pos, w->n, w->stream));
+        pos = r.rdf_pos;
+    }
+    Scratch& s = w->s;
+    int which = 0;
+    CF_CUDA(launch_cell_list_csr(pos, w->n, g, w->ext, T, s, s.cell_off, w->err, &which, w->stream));
+    CF_CUDA(launch_rdf(w->ext, g, w->n, T, bins, r_max, s.pos_sorted, s.keys[which], s.cell_off, r.rdf_acc,
+                       r.type_count, d_hist, w->stream));
+    return CF_OK;
+}
+
+int cf_rdf_backward(cf_world* w, const float* d_pos4, int bins, float r_max, const float* d_ghist, float* d_gpos4)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (w->worlds > 1) return fail(CF_ERR_INVALID, "the radial distribution covers a single world");
+    const int T = w->num_types;
+    if (bins < 1 || !d_ghist || !d_gpos4 || (long long)T * T * bins > kRdfMaxEntries)
+        return fail(CF_ERR_INVALID, "bins must be >= 1 with T * T * bins <= 49152, buffers not NULL");
+    if (!(r_max > 0.0f) || !std::isfinite(r_max)) return fail(CF_ERR_INVALID, "r_max must be finite and positive");
+    rc = ensure_rdf(w);
+    if (rc) return rc;
+    Grid g = choose_step_grid(w->ext, rdf_cutoff(bins, r_max), kMaxCells);
+    apply_worlds(g, 1);
+    rc = ensure_cells(w, g.cells);
+    if (!rc) rc = ensure_offsets(w, g.cells);
+    if (rc) return rc;
+    CF_CUDA(configure_adjoint());
+    Rollout& r = w->ro;
+    const float4* pos = w->pos;
+    if (d_pos4) {
+        CF_CUDA(launch_pack_pos(reinterpret_cast<const float4*>(d_pos4), w->pos, r.rdf_pos, w->n, w->stream));
+        pos = r.rdf_pos;
+    }
+    Scratch& s = w->s;
+    int which = 0;
+    CF_CUDA(launch_cell_list_csr(pos, w->n, g, w->ext, T, s, s.cell_off, w->err, &which, w->stream));
+    CF_CUDA(launch_rdf_grad(w->ext, g, w->n, T, bins, r_max, pos, s.pos_sorted, s.keys[which], s.vals[which],
+                            s.cell_off, d_ghist, r.type_count, reinterpret_cast<float4*>(d_gpos4), w->stream));
+    return CF_OK;
 }
 
 }  // extern "C"

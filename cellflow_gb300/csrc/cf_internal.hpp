@@ -107,6 +107,45 @@ struct Scratch {
     int* n_items = nullptr;
 };
 
+// Differentiable rollout: checkpoints, one segment of replayed states, the
+// adjoint buffers and the record of the last forward (cf_rollout_*).
+struct Rollout {
+    int n_cap = 0;     // particles the buffers hold
+    int ckpt_cap = 0;  // checkpoint states allocated
+    int seg_cap = 0;   // segment states allocated (checkpoint_every + 1)
+    float4* ckpt_pos = nullptr;
+    float4* ckpt_vel = nullptr;
+    int* ckpt_cnt = nullptr;
+    float4* seg_pos = nullptr;
+    float4* seg_vel = nullptr;
+    int* seg_cnt = nullptr;
+    float4* fin_pos = nullptr;  // the state after the forward, restored after the backward
+    float4* fin_vel = nullptr;
+    int* fin_cnt = nullptr;
+    float4* gx = nullptr;         // dL/dx of the current step boundary
+    float4* gv = nullptr;         // dL/dv
+    float4* gf_sorted = nullptr;  // dL/df per particle, cell order
+    float4* ga_sorted = nullptr;  // (dL/da, density), cell order
+    double* gacc = nullptr;       // kTableSize table gradients (32-stride), then CF_GRAD_PARAMS
+    // the last forward
+    int steps = 0;
+    int every = 0;
+    int n = 0;
+    cf_step_params params{};
+    uint64_t table_version = 0;
+    float radio[CF_MAX_TYPES] = {};
+    // the backward as one CUDA graph, re-captured when its key changes
+    cudaGraphExec_t bwd_graph = nullptr;
+    StepConsts bwd_key{};
+    int bwd_steps = 0, bwd_every = 0;
+    const void* bwd_bufs = nullptr;
+    // radial distribution scratch
+    float4* rdf_pos = nullptr;
+    double* rdf_acc = nullptr;
+    unsigned long long* type_count = nullptr;
+};
+constexpr int kGradAccEntries = kTableSize + 8;
+
 }  // namespace cf
 
 struct cf_world {
@@ -157,6 +196,7 @@ struct cf_world {
     cudaGraphExec_t batch_graph = nullptr;
     int batch_graph_steps = 0;
     long long batch_graph_kernels = 0;  // kernel nodes of the captured graph
+    cf::Rollout ro;
 };
 
 namespace cf {
@@ -211,6 +251,25 @@ cudaError_t launch_soa_to_aos(const float4* pos, const float4* vel, const float4
                               cudaStream_t st);
 cudaError_t launch_work_counters(const float4* pos, const int* counts, int n, const Grid& canon, uint32_t* pop,
                                  unsigned long long* out, cudaStream_t st);
+
+// Adjoint and radial distribution (adjoint.cu).
+constexpr int kRdfMaxEntries = 49152;  // T * T * bins held in shared memory
+constexpr int kRdfMaxSmem = kRdfMaxEntries * 4;
+float rdf_cutoff(int bins, float r_max);
+size_t rdf_smem_bytes(int T, int bins);
+cudaError_t configure_adjoint();
+cudaError_t launch_adjoint_step(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
+                                const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
+                                const float4* vel, const int* cnt_prev, const int* cnt_new, float4* gx, float4* gv,
+                                float4* gf_sorted, float4* ga_sorted, double* gacc, cudaStream_t st);
+cudaError_t launch_pack_pos(const float4* src, const float4* typesrc, float4* dst, int n, cudaStream_t st);
+cudaError_t launch_rdf(const float* ext, const Grid& g, int n, int T, int bins, float r_max, const float4* pos_sorted,
+                       const uint32_t* keys_sorted, const uint32_t* cell_off, double* acc,
+                       unsigned long long* type_count, float* hist, cudaStream_t st);
+cudaError_t launch_rdf_grad(const float* ext, const Grid& g, int n, int T, int bins, float r_max,
+                            const float4* pos, const float4* pos_sorted, const uint32_t* keys_sorted,
+                            const uint32_t* vals_sorted, const uint32_t* cell_off, const float* ghist,
+                            unsigned long long* type_count, float4* gpos, cudaStream_t st);
 
 // Host helpers (api.cpp).
 Grid choose_step_grid(const float* ext, float r_cut, int max_cells);

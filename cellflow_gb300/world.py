@@ -245,6 +245,36 @@ class ParticleSimulation:
         check(self._lib.cf_work_counters(self._h, C.byref(p), C.byref(c27), C.byref(inter)), "cf_work_counters")
         return c27.value, inter.value
 
+    # ---- differentiable rollout (device pointers, n float4 each) -------------------
+    def rollout_forward(self, params: SimulationParams, steps: int, checkpoint_every: int = 16,
+                        pos4_in: int | None = None, vel4_in: int | None = None, pos4_out: int | None = None,
+                        vel4_out: int | None = None) -> None:
+        """cf_rollout_forward: `steps` steps keeping checkpoints for cf_rollout_backward."""
+        p = params.to_c()
+        vp = lambda x: C.c_void_p(x) if x else None  # noqa: E731
+        check(self._lib.cf_rollout_forward(self._h, C.byref(p), vp(pos4_in), vp(vel4_in), steps, checkpoint_every,
+                                           vp(pos4_out), vp(vel4_out)), "cf_rollout_forward")
+
+    def rollout_backward(self, gpos4: int | None, gvel4: int | None, gpos4_out: int | None,
+                         gvel4_out: int | None) -> tuple[np.ndarray, np.ndarray]:
+        """cf_rollout_backward: fills the device outputs; returns (dL/dF (T, T), dL/dparams in GRAD_PARAMS order)."""
+        T = self.getNumParticleTypes()
+        gF = np.zeros(T * T, dtype=np.float32)
+        gp = np.zeros(len(_lib.GRAD_PARAMS), dtype=np.float32)
+        vp = lambda x: C.c_void_p(x) if x else None  # noqa: E731
+        check(self._lib.cf_rollout_backward(self._h, vp(gpos4), vp(gvel4), vp(gpos4_out), vp(gvel4_out), _ptr(gF),
+                                            T * T, _ptr(gp)), "cf_rollout_backward")
+        return gF.reshape(T, T), gp
+
+    def rdf(self, bins: int, r_max: float, hist: int, pos4: int | None = None) -> None:
+        """cf_rdf into the device buffer `hist` (T * T * bins floats)."""
+        check(self._lib.cf_rdf(self._h, C.c_void_p(pos4) if pos4 else None, bins, r_max, C.c_void_p(hist)),
+              "cf_rdf")
+
+    def rdf_backward(self, bins: int, r_max: float, ghist: int, gpos4: int, pos4: int | None = None) -> None:
+        check(self._lib.cf_rdf_backward(self._h, C.c_void_p(pos4) if pos4 else None, bins, r_max,
+                                        C.c_void_p(ghist), C.c_void_p(gpos4)), "cf_rdf_backward")
+
     # ---- proximity graph -----------------------------------------------------------
     def proximity_edges(self, distance: float, max_conn: int, cap: int | None = None) -> np.ndarray:
         """Edges (i, j) of generateProximityGraph (ParticleSimulation.cu:625-687), shape (E, 2)."""

@@ -282,6 +282,50 @@ int cf_batch_autotune(cf_batch* b, const cf_step_params* p, int steps, int* chos
 int cf_batch_sync(cf_batch* b);
 int cf_batch_set_stream(cf_batch* b, void* cuda_stream);
 
+/* ---- differentiable rollout (no counterpart in the reference) ---------------
+ *
+ * The gradient of a loss of the state after K steps with respect to the
+ * initial positions and velocities, the force table (as cf_set_force_table
+ * sets it) and six step parameters.  Neighbour counts are held constant (their
+ * derivative is zero almost everywhere), the periodic wrap counts as the
+ * identity, and the neighbour sets are recomputed in the backward pass from
+ * states replayed out of checkpoints taken every `checkpoint_every` steps, so
+ * device memory stays O(n (K / checkpoint_every + checkpoint_every)).
+ * Device pointers hold n float4 values (x, y, z, unused), on the world's
+ * device, ordered like the world's particles; types never change and come
+ * from the world. */
+#define CF_GRAD_REPULSION 0
+#define CF_GRAD_ATTRACTION 1
+#define CF_GRAD_K 2
+#define CF_GRAD_FORCE_MULTIPLIER 3
+#define CF_GRAD_BALANCE 4
+#define CF_GRAD_FRICTION 5
+#define CF_GRAD_PARAMS 6
+
+/* Run nsteps steps from (d_pos4_in, d_vel4_in) — either may be NULL to start
+ * from the world's current positions or velocities — with the world's
+ * neighbour counts as the previous counts of the first step, keeping
+ * checkpoints.  The world ends in the state after nsteps steps, also copied
+ * to d_pos4_out / d_vel4_out when they are not NULL. */
+int cf_rollout_forward(cf_world* w, const cf_step_params* p, const float* d_pos4_in, const float* d_vel4_in,
+                       int nsteps, int checkpoint_every, float* d_pos4_out, float* d_vel4_out);
+/* Adjoint of the last cf_rollout_forward: from dL/dx_K and dL/dv_K (either may
+ * be NULL for zero) to dL/dx_0 and dL/dv_0 (device, either may be NULL),
+ * dL/dF (host, T*T row-major, or NULL) and dL/dparams (host, CF_GRAD_PARAMS
+ * values in CF_GRAD_* order, or NULL).  Fails with CF_ERR_INVALID when the
+ * force table, the radii or the particle count changed since the forward.
+ * The world's state is left as the forward left it. */
+int cf_rollout_backward(cf_world* w, const float* d_gpos4, const float* d_gvel4, float* d_gpos4_out,
+                        float* d_gvel4_out, float* grad_force, int grad_force_count, float* grad_params);
+/* Soft type-resolved radial distribution of the positions d_pos4 (NULL: the
+ * world's current ones): bins of width D = r_max / bins, cubic B-spline
+ * weights of support 2 bins each side of the centre (k + 1/2) D, each entry
+ * normalised by N_a (N_b / V) 4 pi c_k^2 D.  d_hist receives T * T * bins
+ * floats [a][b][k] (device).  T * T * bins <= 49152. */
+int cf_rdf(cf_world* w, const float* d_pos4, int bins, float r_max, float* d_hist);
+/* dL/dpos (device, n float4) of L(hist) given d_ghist = dL/dhist (device). */
+int cf_rdf_backward(cf_world* w, const float* d_pos4, int bins, float r_max, const float* d_ghist, float* d_gpos4);
+
 /* ---- measurement ---------------------------------------------------------- */
 
 /* Device time of the step's phases, accumulated over the steps run since

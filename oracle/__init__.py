@@ -39,15 +39,29 @@ class OracleParams(C.Structure):
     ]
 
 
+class Phys64(C.Structure):
+    """cfo_phys64 of cf_adjoint_oracle.c."""
+
+    _fields_ = [
+        ("repulsion", C.c_double), ("attraction", C.c_double), ("k", C.c_double),
+        ("force_multiplier", C.c_double), ("balance", C.c_double), ("friction", C.c_double),
+        ("delta_t", C.c_double), ("max_expected_neighbors", C.c_int),
+    ]
+
+
+# Order of the parameter gradients (cf_adjoint_oracle.c G_* and CF_GRAD_* of the library).
+GRAD_PARAMS = ("repulsion", "attraction", "k", "force_multiplier", "balance", "friction")
+
+
 def build_oracle(force: bool = False) -> Path:
-    """Compile cf_oracle.c with contraction off (every float op rounded on its own)."""
-    src = HERE / "cf_oracle.c"
-    if not force and ORACLE_LIB.exists() and ORACLE_LIB.stat().st_mtime >= src.stat().st_mtime:
+    """Compile cf_oracle.c and cf_adjoint_oracle.c with contraction off (every float op rounded on its own)."""
+    srcs = [HERE / "cf_oracle.c", HERE / "cf_adjoint_oracle.c"]
+    if not force and ORACLE_LIB.exists() and all(ORACLE_LIB.stat().st_mtime >= s.stat().st_mtime for s in srcs):
         return ORACLE_LIB
     BUILD.mkdir(exist_ok=True)
     tmp = ORACLE_LIB.with_suffix(".so.tmp")
     cmd = ["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
-           str(src), "-o", str(tmp), "-lm"]
+           *map(str, srcs), "-o", str(tmp), "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB
@@ -95,6 +109,19 @@ def lib() -> C.CDLL:
         L.cfo_cell_list.restype = None
         L.cfo_c27.argtypes = [C.c_int, vp, vp, vp]
         L.cfo_c27.restype = C.c_double
+        P64 = C.POINTER(Phys64)
+        L.cfo_rollout_f64.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, C.c_int, P64, vp, C.c_int, vp, vp]
+        L.cfo_rollout_f64.restype = None
+        L.cfo_rollout_grad_f64.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, C.c_int, P64, vp, C.c_int, vp, vp,
+                                           vp, vp, vp, vp]
+        L.cfo_rollout_grad_f64.restype = None
+        L.cfo_rollout_grad_traj_f64.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, C.c_int, P64, vp, C.c_int, vp, vp,
+                                                vp, vp, vp, vp]
+        L.cfo_rollout_grad_traj_f64.restype = None
+        L.cfo_rdf_f64.argtypes = [C.c_int, vp, vp, C.c_int, vp, C.c_int, C.c_double, vp]
+        L.cfo_rdf_f64.restype = None
+        L.cfo_rdf_grad_f64.argtypes = [C.c_int, vp, vp, C.c_int, vp, C.c_int, C.c_double, vp, vp]
+        L.cfo_rdf_grad_f64.restype = None
         _oracle = L
     return _oracle
 
@@ -281,4 +308,100 @@ def ref_force_table(raw, num_types, range_, bias, offset) -> np.ndarray:
     rc = ref_lib().cfref_force_table(_p(raw), num_types, range_, bias, offset, _p(out))
     if rc:
         raise ValueError("reference force table supports T <= 10")
+    return out
+
+
+# ---- FP64 differentiable rollout (cf_adjoint_oracle.c)
+
+def _f64(a, shape=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a if shape is None else a.reshape(shape)
+
+
+def eff_table(params, radio, num_types) -> np.ndarray:
+    """Effective radius of every type pair as the FP32 step rounds it (ParticleSimulation.cu:108-110)."""
+    rb = _f32(radio).ravel()[:num_types]
+    one, half = np.float32(1.0), np.float32(0.5)
+    r = np.float32(params.radius) * (one + rb * np.float32(params.ratio_with_lfo))
+    return ((r[:, None] + r[None, :]) * half).astype(np.float32)
+
+
+def phys64(params, **override) -> Phys64:
+    vals = {name: float(getattr(params, name)) for name in GRAD_PARAMS}
+    vals["delta_t"] = float(params.delta_t)
+    vals.update({k: float(v) for k, v in override.items()})
+    return Phys64(vals["repulsion"], vals["attraction"], vals["k"], vals["force_multiplier"], vals["balance"],
+                  vals["friction"], vals["delta_t"], int(params.max_expected_neighbors))
+
+
+def _extent(params) -> np.ndarray:
+    return np.array([params.canvas_width, params.canvas_height, params.canvas_depth], dtype=np.float64)
+
+
+def rollout_f64(pos, vel, types, counts, table, eff, params, steps, **override):
+    """FP64 rollout; returns (pos, vel, counts, min relative distance of any candidate pair to its cutoff,
+    fingerprint of every step's neighbour counts)."""
+    pos, vel = _f64(pos, (-1, 3)).copy(), _f64(vel, (-1, 3)).copy()
+    n = len(pos)
+    T = int(np.asarray(table).shape[0])
+    types = np.ascontiguousarray(types, dtype=np.uint32)
+    cnt = np.ascontiguousarray(counts, dtype=np.int32).copy()
+    F, effa = _f64(table).ravel(), _f32(eff).ravel()
+    ph, ext = phys64(params, **override), _extent(params)
+    margin, fp = C.c_double(np.inf), C.c_uint64(0)
+    lib().cfo_rollout_f64(n, _p(pos), _p(vel), _p(types), _p(cnt), _p(F), _p(effa), T, C.byref(ph), _p(ext), steps,
+                          C.byref(margin), C.byref(fp))
+    return pos, vel, cnt, margin.value, fp.value
+
+
+def rollout_grad_f64(pos, vel, types, counts, table, eff, params, steps, gpos, gvel, **override):
+    """FP64 adjoint of a rollout: (d/dpos0, d/dvel0, d/dF, d/dparams in GRAD_PARAMS order)."""
+    pos, vel = _f64(pos, (-1, 3)), _f64(vel, (-1, 3))
+    n = len(pos)
+    T = int(np.asarray(table).shape[0])
+    types = np.ascontiguousarray(types, dtype=np.uint32)
+    cnt = np.ascontiguousarray(counts, dtype=np.int32)
+    F, effa = _f64(table).ravel(), _f32(eff).ravel()
+    ph, ext = phys64(params, **override), _extent(params)
+    gp, gv = _f64(gpos, (-1, 3)), _f64(gvel, (-1, 3))
+    g0, gv0 = np.zeros((n, 3)), np.zeros((n, 3))
+    gF, gph = np.zeros(T * T), np.zeros(len(GRAD_PARAMS))
+    lib().cfo_rollout_grad_f64(n, _p(pos), _p(vel), _p(types), _p(cnt), _p(F), _p(effa), T, C.byref(ph), _p(ext),
+                               steps, _p(gp), _p(gv), _p(g0), _p(gv0), _p(gF), _p(gph))
+    return g0, gv0, gF.reshape(T, T), gph
+
+
+def rollout_grad_traj_f64(P, V, Cn, types, table, eff, params, gpos, gvel, **override):
+    """FP64 adjoint along a given trajectory: P, V of shape (K+1, n, 3), Cn of shape (K+1, n)."""
+    P, V = _f64(P), _f64(V)
+    steps, n = P.shape[0] - 1, P.shape[1]
+    T = int(np.asarray(table).shape[0])
+    types = np.ascontiguousarray(types, dtype=np.uint32)
+    Cn = np.ascontiguousarray(Cn, dtype=np.int32)
+    F, effa = _f64(table).ravel(), _f32(eff).ravel()
+    ph, ext = phys64(params, **override), _extent(params)
+    gp, gv = _f64(gpos, (-1, 3)), _f64(gvel, (-1, 3))
+    g0, gv0 = np.zeros((n, 3)), np.zeros((n, 3))
+    gF, gph = np.zeros(T * T), np.zeros(len(GRAD_PARAMS))
+    lib().cfo_rollout_grad_traj_f64(n, _p(P), _p(V), _p(Cn), _p(types), _p(F), _p(effa), T, C.byref(ph), _p(ext),
+                                    steps, _p(gp), _p(gv), _p(g0), _p(gv0), _p(gF), _p(gph))
+    return g0, gv0, gF.reshape(T, T), gph
+
+
+def rdf_f64(pos, types, num_types, extent, bins, r_max) -> np.ndarray:
+    """Soft type-resolved radial distribution, shape (T, T, bins)."""
+    pos = _f64(pos, (-1, 3))
+    types = np.ascontiguousarray(types, dtype=np.uint32)
+    ext = _f64(extent)
+    h = np.zeros(num_types * num_types * bins)
+    lib().cfo_rdf_f64(len(pos), _p(pos), _p(types), num_types, _p(ext), bins, r_max, _p(h))
+    return h.reshape(num_types, num_types, bins)
+
+
+def rdf_grad_f64(pos, types, num_types, extent, bins, r_max, ghist) -> np.ndarray:
+    pos = _f64(pos, (-1, 3))
+    types = np.ascontiguousarray(types, dtype=np.uint32)
+    ext, g = _f64(extent), _f64(ghist).ravel()
+    out = np.zeros_like(pos)
+    lib().cfo_rdf_grad_f64(len(pos), _p(pos), _p(types), num_types, _p(ext), bins, r_max, _p(g), _p(out))
     return out
