@@ -187,7 +187,13 @@ def run_reference_arm(args, rank, world):
         radio = np.zeros(bw.num_types, np.float32)
         full_n = total_n
     else:
-        w = inputs.WORKLOADS[args.workload]
+        if args.workload in ROLLOUT:
+            # the reference has no adjoint: its step on the rollout's configuration
+            cfg = ROLLOUT[args.workload]
+            w = inputs.Workload(args.workload, n=cfg["n"], num_types=cfg["types"], radius=cfg["radius"],
+                                steps=cfg["steps"], seed=cfg["seed"])
+        else:
+            w = inputs.WORKLOADS[args.workload]
         params = w.params()
         p0, t0_, tab0 = w.positions(), w.types(), w.table()
         fixed = (p0, t0_, tab0, oracle.to_records(p0, np.zeros_like(p0), t0_))
@@ -549,6 +555,131 @@ def run_batched(args, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
+ROLLOUT = {"rollout_n16k_k64": dict(n=16384, types=6, radius=0.1, steps=64, every=16, bins=32, r_max=0.2,
+                                    seed=0x5EED0005)}
+
+
+def run_rollout(args, rank, world, local):
+    """--workload rollout_n16k_k64: the differentiable rollout.  One bench step is one
+    forward + backward pass of the K-step rollout with the soft radial distribution loss
+    (cf_rollout_forward, cf_rdf, cf_rdf_backward, cf_rollout_backward); the plain step
+    (cf_step, K steps) is timed beside it for the adjoint / forward cost ratio."""
+    import numpy as np
+    import torch
+
+    import cellflow_gb300 as cf
+    from cellflow_gb300 import _lib, inputs
+    from cellflow_gb300.world import ParticleSimulation
+
+    torch.cuda.set_device(local)
+    cfg = ROLLOUT[args.workload]
+    n, T, K = cfg["n"], cfg["types"], cfg["steps"]
+    w = inputs.Workload(args.workload, n=n, num_types=T, radius=cfg["radius"], steps=K, seed=cfg["seed"])
+    params = w.params()
+    pos, types, table = w.positions(), w.types(), w.table()
+    target_table = inputs.gaussian_table(T, 0.0, 0.5, cfg["seed"] + 1)
+    stream = torch.cuda.Stream()
+    sim = ParticleSimulation(n, T, w.extent, w.extent, w.extent)
+    sim.set_stream(stream.cuda_stream)
+    sim.set_particles(pos, types)
+    sim.setRadioByType(np.zeros(T, np.float32))
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    lib = _lib.load()
+    bins, r_max = cfg["bins"], cfg["r_max"]
+    with torch.cuda.stream(stream):
+        hist = torch.empty((T, T, bins), dtype=torch.float32, device="cuda")
+        target = torch.empty_like(hist)
+        ghist = torch.empty_like(hist)
+        pos4 = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        pos4[:, :3] = torch.from_numpy(pos).cuda()
+        vel4 = torch.zeros_like(pos4)
+        xk, vk, gx, g0, gv0 = (torch.empty_like(pos4) for _ in range(5))
+    stream.synchronize()
+    # target: the radial distribution after K steps under the hidden table
+    sim.setForceTable(target_table)
+    sim.rollout_forward(params, K, cfg["every"], pos4.data_ptr(), vel4.data_ptr(), xk.data_ptr(), None)
+    sim.rdf(bins, r_max, target.data_ptr(), xk.data_ptr())
+    sim.sync()
+    sim.setForceTable(table)
+    s0 = sim.get_state()
+
+    def train_step():
+        sim.rollout_forward(params, K, cfg["every"], pos4.data_ptr(), vel4.data_ptr(), xk.data_ptr(), None)
+        sim.rdf(bins, r_max, hist.data_ptr(), xk.data_ptr())
+        with torch.cuda.stream(stream):
+            torch.sub(hist, target, out=ghist).mul_(2.0 / hist.numel())
+        sim.rdf_backward(bins, r_max, ghist.data_ptr(), gx.data_ptr(), xk.data_ptr())
+        return sim.rollout_backward(gx.data_ptr(), None, g0.data_ptr(), gv0.data_ptr())
+
+    def timed(fn, reps):
+        ms = []
+        for _ in range(reps):
+            sim.set_state(*s0)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms
+
+    for _ in range(max(args.warmup, 3)):
+        sim.set_state(*s0)
+        train_step()
+    sim.sync()
+    reps = max(1, args.steps // 10) if args.steps >= 10 else args.steps
+    clocks = ClockSampler(local)
+    clocks.start()
+    fwd_plain = timed(lambda: sim.simulate(params, K), reps)
+    fwd_roll = timed(lambda: sim.rollout_forward(params, K, cfg["every"], None, None, None, None), reps)
+    bwd = timed(lambda: sim.rollout_backward(gx.data_ptr(), None, g0.data_ptr(), gv0.data_ptr()), reps)
+    train = timed(train_step, reps)
+    clk = clocks.stop()
+    med = statistics.median
+    step_fwd = med(fwd_plain) / K
+    step_bwd = med(bwd) / K
+    value = n * K / (med(train) * 1e-3)
+    # end to end: host positions in, gradients out (pinned), one training pass
+    hpos = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    hpos[:, :3] = torch.from_numpy(pos)
+    hgrad = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    e2e = []
+    for _ in range(reps):
+        sim.set_state(*s0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            pos4.copy_(hpos, non_blocking=True)
+        gF, gp = train_step()  # reads the table and parameter gradients back (synchronises)
+        with torch.cuda.stream(stream):
+            hgrad.copy_(g0, non_blocking=True)
+        stream.synchronize()
+        e2e.append(time.perf_counter() - t0)
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": reps, "warmup": max(args.warmup, 3), "ms_per_step": med(train),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Philox4x32-10): uniform positions, N(0,0.5) table, hidden N(0,0.5) target "
+                    "table",
+            "config": {"workload": args.workload, "n": n, "types": T, "radius": cfg["radius"], "rollout_steps": K,
+                       "checkpoint_every": cfg["every"], "loss": f"MSE of the soft radial distribution "
+                       f"({bins} bins, r <= {r_max})", "l2": "state smaller than L2; 256 MiB flush before each "
+                       "timed pass"},
+            "unit_of_step": "one forward + backward pass of the K-step rollout and its loss",
+            "forward_step_ms": step_fwd, "rollout_forward_step_ms": med(fwd_roll) / K,
+            "adjoint_step_ms": step_bwd, "adjoint_over_forward": step_bwd / step_fwd,
+            "e2e": {"value": n * K / med(e2e), "unit": "particle-steps/s", "h2d_bytes_per_step": n * 16,
+                    "d2h_bytes_per_step": n * 16 + 4 * (T * T + 6),
+                    "path": "pinned positions in, rollout + loss + adjoint, pinned position gradients out"},
+            "gpu_launches": None, "clocks": clk,
+            "library": cf.__name__ + ": " + lib.cf_version().decode(),
+        }
+        print(json.dumps(line), flush=True)
+
+
 def reference_gpu_kernel(w, params, pos, types, table, radio, stream):
     """The reference step kernel (sm_103a build of ParticleSimulation.cu:69-166) on the same
     inputs, launched as ParticleSimulation::simulate does; a few steps, CUDA events."""
@@ -604,6 +735,9 @@ def main():
 
     if args.workload in inputs.BATCHED:
         run_batched(args, rank, world, local)
+        return
+    if args.workload in ROLLOUT:
+        run_rollout(args, rank, world, local)
         return
     run_gb300(args, rank, world, local)
 

@@ -92,6 +92,7 @@ int alloc_particles(cf_world* w)
         CF_CUDA(dev_alloc(&s.vals[b], n));
     }
     CF_CUDA(dev_alloc(&s.pos_sorted, n));
+    CF_CUDA(dev_alloc(&s.aux, n));
     s.hist_cap = radix_hist_entries(n);
     CF_CUDA(dev_alloc(&s.hist, s.hist_cap));
     s.scan_tmp_cap = std::max(scan_tmp_entries((int)s.hist_cap), scan_tmp_entries(n + 1));
@@ -127,6 +128,8 @@ void free_particles(cf_world* w)
         dev_free(s.vals[b]);
     }
     dev_free(s.pos_sorted);
+    dev_free(s.aux);
+    dev_free(s.tile_sums);
     dev_free(s.hist);
     dev_free(s.scan_tmp);
     dev_free(s.cell_start);
@@ -167,9 +170,18 @@ int ensure_offsets(cf_world* w, int cells)
 {
     Scratch& s = w->s;
     const size_t need_tmp = scan_tmp_entries(cells + 1);
-    if ((size_t)cells + 1 <= s.off_cap && need_tmp <= s.scan_tmp_cap) return CF_OK;
+    // tiles of the CSR build: every tile holds more than kTileCellsMax / 2 cells
+    const size_t need_tiles = (size_t)cells / (kTileCellsMax / 2) + 2;
+    if ((size_t)cells + 1 <= s.off_cap && need_tmp <= s.scan_tmp_cap && need_tiles <= s.tiles_cap) return CF_OK;
     CF_CUDA(cudaStreamSynchronize(w->stream));
     drop_graphs(w);
+    if (need_tiles > s.tiles_cap) {
+        dev_free(s.tile_sums);
+        s.tile_sums = nullptr;
+        s.tiles_cap = 0;
+        CF_CUDA(dev_alloc(&s.tile_sums, need_tiles));
+        s.tiles_cap = need_tiles;
+    }
     if ((size_t)cells + 1 > s.off_cap) {
         dev_free(s.cell_off);
         s.cell_off = nullptr;
@@ -406,9 +418,8 @@ int enqueue_step(cf_world* w, const StepConsts& c, int prof)
     if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[0], w->stream, cudaEventRecordExternal));
     int which = 0;
     Scratch& s = w->s;
-    CF_CUDA(launch_cell_list_csr(w->pos, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, w->err, &which,
-                                 w->stream));
-    CF_CUDA(launch_step_plan(s.cell_off, w->n, c.grid, s.items, s.n_items, w->stream));
+    CF_CUDA(launch_cell_list_csr(w->pos, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, s.items, s.n_items, w->err,
+                                 &which, w->stream));
     if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[1], w->stream, cudaEventRecordExternal));
     CF_CUDA(launch_step_force(c, w->tables, s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.items,
                               s.n_items, max_step_items(w->n, c.grid), w->pos, w->vel, w->acc, w->counts,
@@ -979,7 +990,7 @@ int cf_step(cf_world* w, const cf_step_params* p, int nsteps)
         rc = step_graph(w, c, prof, &exec);
         if (rc) return rc;
     }
-    const long long launches = cell_list_csr_launches(w->n, c.grid.key_bits, c.grid.cells) + step_launches(w->n);
+    const long long launches = cell_list_csr_launches(w->n, c.grid, true) + step_launches(w->n);
     for (int s = 0; s < nsteps; s++) {
         if (exec)
             CF_CUDA(cudaGraphLaunch(exec, w->stream));
@@ -1151,8 +1162,8 @@ int cf_debug_cell_list(cf_world* w, const cf_step_params* p, uint32_t* cell_of, 
     if (rc) return rc;
     // the step's own cell list: CSR offsets, stable radix order
     int which = 0;
-    CF_CUDA(launch_cell_list_csr(w->pos, w->n, c.grid, c.ext, w->num_types, w->s, w->s.cell_off, w->err, &which,
-                                 w->stream));
+    CF_CUDA(launch_cell_list_csr(w->pos, w->n, c.grid, c.ext, w->num_types, w->s, w->s.cell_off, nullptr, nullptr,
+                                 w->err, &which, w->stream));
     // the hash wrote cell ids in original order into keys[0] before sorting;
     // recompute them (the sort may have reused that buffer)
     CF_CUDA(launch_cell_hash(w->pos, w->n, c.grid, c.ext, w->num_types, w->s.keys[which ^ 1], w->err, w->stream));
@@ -1635,8 +1646,8 @@ int enqueue_rollout_backward(cf_world* w, const StepConsts& c)
                                 w->stream));
         for (int t = len - 1; t >= 0; t--) {
             int which = 0;
-            CF_CUDA(launch_cell_list_csr(r.seg_pos + n * t, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, w->err,
-                                         &which, w->stream));
+            CF_CUDA(launch_cell_list_csr(r.seg_pos + n * t, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, nullptr,
+                                         nullptr, w->err, &which, w->stream));
             CF_CUDA(launch_adjoint_step(c, w->tables, s.pos_sorted, s.keys[which], s.vals[which], s.cell_off,
                                         r.seg_vel + n * t, r.seg_cnt + n * t, r.seg_cnt + n * (t + 1), r.gx, r.gv,
                                         r.gf_sorted, r.ga_sorted, r.gacc, w->stream));
@@ -1802,7 +1813,7 @@ int cf_rdf(cf_world* w, const float* d_pos4, int bins, float r_max, float* d_his
     }
     Scratch& s = w->s;
     int which = 0;
-    CF_CUDA(launch_cell_list_csr(pos, w->n, g, w->ext, T, s, s.cell_off, w->err, &which, w->stream));
+    CF_CUDA(launch_cell_list_csr(pos, w->n, g, w->ext, T, s, s.cell_off, nullptr, nullptr, w->err, &which, w->stream));
     CF_CUDA(launch_rdf(w->ext, g, w->n, T, bins, r_max, s.pos_sorted, s.keys[which], s.cell_off, r.rdf_acc,
                        r.type_count, d_hist, w->stream));
     return CF_OK;
@@ -1833,7 +1844,7 @@ int cf_rdf_backward(cf_world* w, const float* d_pos4, int bins, float r_max, con
     }
     Scratch& s = w->s;
     int which = 0;
-    CF_CUDA(launch_cell_list_csr(pos, w->n, g, w->ext, T, s, s.cell_off, w->err, &which, w->stream));
+    CF_CUDA(launch_cell_list_csr(pos, w->n, g, w->ext, T, s, s.cell_off, nullptr, nullptr, w->err, &which, w->stream));
     CF_CUDA(launch_rdf_grad(w->ext, g, w->n, T, bins, r_max, pos, s.pos_sorted, s.keys[which], s.vals[which],
                             s.cell_off, d_ghist, r.type_count, reinterpret_cast<float4*>(d_gpos4), w->stream));
     return CF_OK;

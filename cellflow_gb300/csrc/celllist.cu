@@ -44,10 +44,13 @@ __global__ void __launch_bounds__(kThreads)
 
 // Cell id of every particle (world * cells_w + cell) and the population of
 // every cell (counts must be zero on entry); flags positions outside the box,
-// types outside [0, T) and world indices outside the batch.
+// types outside [0, T) and world indices outside the batch.  With slot, the
+// particle's arrival slot in its cell (unordered: it only places the
+// particle for the stable ranking that follows).
 __global__ void __launch_bounds__(kThreads)
     cell_hash_count_kernel(const float4* __restrict__ pos, int n, Grid g, float ex, float ey, float ez, int num_types,
-                           uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, int* __restrict__ err)
+                           uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, uint32_t* __restrict__ slot,
+                           int* __restrict__ err)
 {
     int i = blockIdx.x * kThreads + threadIdx.x;
     if (i >= n) return;
@@ -63,7 +66,8 @@ __global__ void __launch_bounds__(kThreads)
     int cz = cell_coord(p.z, g.inv[2], g.m[2]);
     const uint32_t key = world * (uint32_t)g.cells_w + (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
     keys[i] = key;
-    atomicAdd(&counts[key], 1u);
+    const uint32_t s = atomicAdd(&counts[key], 1u);
+    if (slot) slot[i] = s;
 }
 
 // The position snapshot in sorted (cell) order.
@@ -245,6 +249,188 @@ __global__ void __launch_bounds__(kThreads)
     pos_sorted[t] = pos[vals[t]];
 }
 
+// ---- CSR cell list with the force kernel's plan ------------------------------
+//
+// After the hash (populations by atomics, each particle's arrival slot):
+//   tile_reduce  per tile of whole cell rows: its particles and its items
+//                (32-particle chunks of each row, the force kernel's work units)
+//   tile_apply   per tile: the totals of the tiles before it (summed by the
+//                block, a few hundred values at most), then the tile's CSR
+//                offsets and its rows' items
+//   place        particle i to offset[cell] + slot (unordered within a cell)
+//   rank_gather  the stable position of every particle: its cell's start plus
+//                the number of particles of that cell with a smaller index;
+//                writes sorted values, keys and the position snapshot
+// No kernel waits on another block.
+
+constexpr int kTileThreads = 512;
+constexpr int kTileItems = kTileCellsMax / kTileThreads;  // cells (and rows) per thread at most
+constexpr int kTileWarps = kTileThreads / 32;
+
+struct TileGeom {
+    int m0;             // cells per row
+    int rows;           // rows of the whole grid (all worlds)
+    int rows_per_tile;  // whole rows per tile: floor(kTileCellsMax / m0) >= 1
+    int tiles;
+};
+
+// Exclusive scan of one value per thread over a kTileThreads block.
+__device__ __forceinline__ uint32_t tile_block_scan(uint32_t v, uint32_t* total, uint32_t* warp_sums)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t s = lane < kTileWarps ? warp_sums[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < kTileWarps; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < kTileWarps) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const uint32_t before = warp ? warp_sums[warp - 1] : 0u;
+    *total = warp_sums[kTileWarps - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+// The tile's local CSR offsets (s_off[0..tc], s_off[tc] = its particles) and
+// each thread's first local item with the tile's item total.
+struct TileLocal {
+    int c0, tc, r0, nr;   // first cell, cells, first row, rows
+    uint32_t particles;   // of the tile
+    uint32_t items;       // of the tile
+    uint32_t item_before; // local items before this thread's rows
+    int rk;               // rows per thread
+};
+
+__device__ __forceinline__ TileLocal tile_local(const uint32_t* __restrict__ counts, const TileGeom& tg, int t,
+                                                uint32_t* s_off, uint32_t* warp_sums)
+{
+    TileLocal L;
+    L.r0 = t * tg.rows_per_tile;
+    L.nr = min(tg.rows_per_tile, tg.rows - L.r0);
+    L.c0 = L.r0 * tg.m0;
+    L.tc = L.nr * tg.m0;
+    const int j0 = threadIdx.x * kTileItems;
+    uint32_t v[kTileItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kTileItems; k++) {
+        v[k] = j0 + k < L.tc ? counts[L.c0 + j0 + k] : 0u;
+        sum += v[k];
+    }
+    uint32_t run = tile_block_scan(sum, &L.particles, warp_sums);
+#pragma unroll
+    for (int k = 0; k < kTileItems; k++) {
+        if (j0 + k < L.tc) s_off[j0 + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 0) s_off[L.tc] = L.particles;
+    __syncthreads();
+    L.rk = (L.nr + kTileThreads - 1) / kTileThreads;
+    uint32_t chunks = 0;
+    for (int q = 0; q < L.rk; q++) {
+        const int r = threadIdx.x * L.rk + q;
+        if (r < L.nr) chunks += (s_off[(r + 1) * tg.m0] - s_off[r * tg.m0] + 31u) / 32u;
+    }
+    L.item_before = tile_block_scan(chunks, &L.items, warp_sums);
+    return L;
+}
+
+__global__ void __launch_bounds__(kTileThreads)
+    tile_reduce_kernel(const uint32_t* __restrict__ counts, TileGeom tg, uint2* __restrict__ tile_sums)
+{
+    __shared__ uint32_t s_off[kTileCellsMax + 1];
+    __shared__ uint32_t warp_sums[kTileWarps];
+    const TileLocal L = tile_local(counts, tg, blockIdx.x, s_off, warp_sums);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = make_uint2(L.particles, L.items);
+}
+
+__global__ void __launch_bounds__(kTileThreads)
+    tile_apply_kernel(uint32_t* cell_off, TileGeom tg, const uint2* __restrict__ tile_sums, int2* __restrict__ items,
+                      int* __restrict__ n_items)
+{
+    __shared__ uint32_t s_off[kTileCellsMax + 1];
+    __shared__ uint32_t warp_sums[kTileWarps];
+    __shared__ uint32_t s_prefix[2][kTileWarps];
+    // totals of the tiles before this one
+    uint32_t pp = 0, pi = 0;
+    for (int q = threadIdx.x; q < (int)blockIdx.x; q += kTileThreads) {
+        const uint2 s = tile_sums[q];
+        pp += s.x;
+        pi += s.y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        pp += __shfl_xor_sync(0xffffffffu, pp, o);
+        pi += __shfl_xor_sync(0xffffffffu, pi, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_prefix[0][warp] = pp;
+        s_prefix[1][warp] = pi;
+    }
+    // cell_off holds the populations on entry: this tile reads its own cells
+    // (into shared memory) before any block writes offsets over them, and no
+    // block reads another tile's cells
+    const TileLocal L = tile_local(cell_off, tg, blockIdx.x, s_off, warp_sums);
+    uint32_t prefix_p = 0, prefix_i = 0;
+#pragma unroll
+    for (int w = 0; w < kTileWarps; w++) {
+        prefix_p += s_prefix[0][w];
+        prefix_i += s_prefix[1][w];
+    }
+    for (int k = threadIdx.x; k < L.tc; k += kTileThreads) cell_off[L.c0 + k] = prefix_p + s_off[k];
+    const bool last = (int)blockIdx.x == tg.tiles - 1;
+    if (last && threadIdx.x == 0) cell_off[L.c0 + L.tc] = prefix_p + L.particles;
+    if (!items) return;
+    uint32_t item = prefix_i + L.item_before;
+    for (int q = 0; q < L.rk; q++) {
+        const int r = threadIdx.x * L.rk + q;
+        if (r >= L.nr) break;
+        const uint32_t start = prefix_p + s_off[r * tg.m0];
+        const uint32_t cnt = s_off[(r + 1) * tg.m0] - s_off[r * tg.m0];
+        for (uint32_t k = 0; k < cnt; k += 32u) items[item++] = make_int2((int)(start + k), (int)min(32u, cnt - k));
+    }
+    if (last && threadIdx.x == 0) *n_items = (int)(prefix_i + L.items);
+}
+
+__global__ void __launch_bounds__(kThreads)
+    place_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ slot,
+                 const uint32_t* __restrict__ cell_off, int n, uint32_t* __restrict__ unsorted)
+{
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i < n) unsorted[cell_off[keys[i]] + slot[i]] = (uint32_t)i;
+}
+
+__global__ void __launch_bounds__(kThreads)
+    rank_gather_kernel(const uint32_t* __restrict__ unsorted, const uint32_t* __restrict__ keys,
+                       const uint32_t* __restrict__ cell_off, const float4* __restrict__ pos, int n,
+                       uint32_t* __restrict__ vals_sorted, uint32_t* __restrict__ keys_sorted,
+                       float4* __restrict__ pos_sorted)
+{
+    const int p = blockIdx.x * kThreads + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t i = unsorted[p];
+    const uint32_t key = keys[i];
+    const uint32_t b = cell_off[key], e = cell_off[key + 1];
+    uint32_t rank = 0;
+    for (uint32_t q = b; q < e; q++) rank += unsorted[q] < i ? 1u : 0u;
+    const uint32_t dst = b + rank;
+    vals_sorted[dst] = i;
+    keys_sorted[dst] = key;
+    pos_sorted[dst] = pos[i];
+}
+
 // ---- work counters ---------------------------------------------------------
 
 // Cell of a particle in the work-model grid of its own world (world-major).
@@ -420,38 +606,61 @@ cudaError_t launch_cell_bounds(const uint32_t* keys, const uint32_t* vals, int n
 // Cell list in CSR form for the step: keys[0] = cell ids, radix-sorted
 // (keys, vals)[*which], cell_off[c] = particles in cells < c (cells + 1
 // entries), pos_sorted = positions in sorted order.
-cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
-                                 Scratch& s, uint32_t* cell_off, int* err, int* which, cudaStream_t st)
+int cell_list_tiles(const Grid& g)
 {
-    *which = 0;
-    cudaError_t e = cudaMemsetAsync(cell_off, 0, sizeof(uint32_t) * ((size_t)g.cells + 1), st);
-    if (e != cudaSuccess) return e;
-    if (n > 0) {
-        cell_hash_count_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(pos, n, g, ext[0], ext[1], ext[2],
-                                                                            num_types, s.keys[0], cell_off, err);
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-    }
-    e = launch_radix_sort(s, n, g.key_bits, which, st);
-    if (e != cudaSuccess) return e;
-    e = launch_scan_exclusive(cell_off, cell_off, g.cells + 1, s.scan_tmp, s.scan_tmp_cap, st);
-    if (e != cudaSuccess) return e;
-    if (n > 0) {
-        gather_sorted_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.vals[*which], n, pos, s.pos_sorted);
-        e = cudaGetLastError();
-    }
-    return e;
+    if (g.m[0] > kTileCellsMax) return 0;
+    const int rows = g.cells / g.m[0];
+    const int per = kTileCellsMax / g.m[0];
+    return (rows + per - 1) / per;
 }
 
-int cell_list_csr_launches(int n, int key_bits, int cells)
+cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
+                                 Scratch& s, uint32_t* cell_off, int2* items, int* n_items, int* err, int* which,
+                                 cudaStream_t st)
 {
-    if (n <= 0) return 0;
-    int passes = (key_bits + 7) / 8;
-    if (passes < 1) passes = 1;
-    int entries = (int)radix_hist_entries(n);
-    int scan = blocks_for(entries, kScanTile) == 1 ? 1 : 3;
-    int cscan = blocks_for(cells + 1, kScanTile) == 1 ? 1 : 3;
-    return 1 + passes * (2 + scan) + cscan + 1;
+    cudaError_t e = cudaMemsetAsync(cell_off, 0, sizeof(uint32_t) * ((size_t)g.cells + 1), st);
+    if (e != cudaSuccess) return e;
+    const int tiles = cell_list_tiles(g);
+    if (n > 0)
+        cell_hash_count_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(
+            pos, n, g, ext[0], ext[1], ext[2], num_types, s.keys[0], cell_off, tiles ? s.aux : nullptr, err);
+    if (!tiles) {
+        // rows longer than a tile: stable radix sort of the cell ids, device-wide scan
+        e = launch_radix_sort(s, n, g.key_bits, which, st);
+        if (e == cudaSuccess) e = launch_scan_exclusive(cell_off, cell_off, g.cells + 1, s.scan_tmp, s.scan_tmp_cap, st);
+        if (e == cudaSuccess && n > 0)
+            gather_sorted_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.vals[*which], n, pos, s.pos_sorted);
+        if (e == cudaSuccess && items) e = launch_step_plan(cell_off, n, g, items, n_items, st);
+        return e == cudaSuccess ? cudaGetLastError() : e;
+    }
+    TileGeom tg;
+    tg.m0 = g.m[0];
+    tg.rows = g.cells / g.m[0];
+    tg.rows_per_tile = kTileCellsMax / g.m[0];
+    tg.tiles = tiles;
+    tile_reduce_kernel<<<tiles, kTileThreads, 0, st>>>(cell_off, tg, s.tile_sums);
+    tile_apply_kernel<<<tiles, kTileThreads, 0, st>>>(cell_off, tg, s.tile_sums, items, n_items);
+    *which = 1;
+    if (n > 0) {
+        place_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.keys[0], s.aux, cell_off, n, s.vals[0]);
+        rank_gather_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.vals[0], s.keys[0], cell_off, pos, n,
+                                                                         s.vals[1], s.keys[1], s.pos_sorted);
+    }
+    return cudaGetLastError();
+}
+
+int cell_list_csr_launches(int n, const Grid& g, bool with_plan)
+{
+    if (cell_list_tiles(g) == 0) {
+        if (n <= 0) return with_plan ? 0 : 0;
+        int passes = (g.key_bits + 7) / 8;
+        if (passes < 1) passes = 1;
+        int entries = (int)radix_hist_entries(n);
+        int scan = blocks_for(entries, kScanTile) == 1 ? 1 : 3;
+        int cscan = blocks_for(g.cells + 1, kScanTile) == 1 ? 1 : 3;
+        return 1 + passes * (2 + scan) + cscan + 1 + (with_plan ? 1 : 0);
+    }
+    return 2 + (n > 0 ? 3 : 0);  // tile reduce and apply; hash, place, rank
 }
 
 cudaError_t launch_work_counters(const float4* pos, const int* counts, int n, const Grid& canon, uint32_t* pop,

@@ -105,7 +105,14 @@ struct Scratch {
     int2* items = nullptr;       // (first sorted index, particles) per item
     size_t items_cap = 0;
     int* n_items = nullptr;
+    // tiled CSR build: arrival slot per particle, per-tile totals
+    uint32_t* aux = nullptr;  // n
+    uint2* tile_sums = nullptr;
+    size_t tiles_cap = 0;
 };
+
+// Cells of one tile of the CSR build (whole rows; 16 KB of shared memory).
+constexpr int kTileCellsMax = 4096;
 
 // Differentiable rollout: checkpoints, one segment of replayed states, the
 // adjoint buffers and the record of the last forward (cf_rollout_*).
@@ -231,9 +238,16 @@ cudaError_t launch_scan_exclusive(const uint32_t* in, uint32_t* out, int n, uint
 size_t scan_tmp_entries(int n);
 size_t radix_hist_entries(int n);
 int cell_list_launches(int n, int key_bits);
+// The step's cell list: CSR offsets (cells + 1), sorted keys / values
+// (s.keys[*which], s.vals[*which], stable: cell order, ties in index order),
+// the position snapshot s.pos_sorted and, when items is not null, the force
+// kernel's row-aligned items.  Rows of at most kTileCellsMax cells take the
+// tiled path (5 kernels); longer rows a radix sort.
 cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
-                                 Scratch& s, uint32_t* cell_off, int* err, int* which, cudaStream_t st);
-int cell_list_csr_launches(int n, int key_bits, int cells);
+                                 Scratch& s, uint32_t* cell_off, int2* items, int* n_items, int* err, int* which,
+                                 cudaStream_t st);
+int cell_list_csr_launches(int n, const Grid& g, bool with_plan);
+int cell_list_tiles(const Grid& g);  // 0 when the rows are longer than a tile
 cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* keys_sorted,
                                     const uint32_t* vals_sorted, const uint32_t* cell_start,
                                     const uint32_t* cell_end, const Grid& g, int n, float dsq, int max_conn,

@@ -474,7 +474,7 @@ cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const 
 
 int max_step_items(int n, const Grid& g) { return (n + 31) / 32 + g.worlds * g.m[1] * g.m[2]; }
 
-int step_launches(int n) { return n > 0 ? 2 : 0; }
+int step_launches(int n) { return n > 0 ? 1 : 0; }  // the force kernel (the plan is part of the cell list)
 
 cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, int2* items, int* n_items,
                              cudaStream_t st)
