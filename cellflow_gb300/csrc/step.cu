@@ -87,13 +87,19 @@ struct Lane {
     int count;
 };
 
+// Per type pair of the item's world, T-stride: (R F, A F / eff).  With
+// s = d^2 + 1e-4 and rs = 1/sqrt(s), the reference's term
+//   (d / dist) F (R exp(-k r^2) - A r),  r = dist / eff   (ParticleSimulation.cu:113-124)
+// is  d * rs * (R F * exp2(c1 s) - (A F / eff) * s rs),  c1 = -k log2(e) / eff^2.
 struct Tables {
-    const float* force;  // the item's world, T-stride
-    const float* inv_eff;
+    const float2* coef;  // (R F, A F / eff), T-stride
+    const float* c1;     // 32-stride (unused with a uniform radius)
     const float* thr;
     const float* thr_lo;
     int T;
 };
+
+constexpr float kLog2e = 1.4426950408889634f;
 
 // Displacement from the home to a staged candidate: the filter's arithmetic.
 template <bool kGeneric>
@@ -111,14 +117,15 @@ __device__ __forceinline__ void staged_delta(const StepConsts& c, float cx, floa
     }
 }
 
-// One queued pair: certain-interaction bound, exact fallback, force term.
+// One queued pair's interaction test: certain-interaction bound, exact
+// fallback.  Returns the staged displacement and its contracted d^2.
 template <bool kGeneric, bool kUniformR>
-__device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float cx, float cy, float cz,
-                                           uint32_t meta, const float4* __restrict__ pos_sorted, const Tables& tb)
+__device__ __forceinline__ bool pair_test(const StepConsts& c, const Lane& L, float cx, float cy, float cz,
+                                          uint32_t meta, const float4* __restrict__ pos_sorted, const Tables& tb,
+                                          float& dx, float& dy, float& dz, float& d2)
 {
-    float dx, dy, dz;
     staged_delta<kGeneric>(c, cx, cy, cz, L.h, dx, dy, dz);
-    const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     const uint32_t other = meta >> kTypeShift;
     const uint32_t pair = L.tp * kTableStride + other;
     bool inter = d2 < (kUniformR ? c.thr_lo_uniform : tb.thr_lo[pair]);
@@ -138,18 +145,30 @@ __device__ __forceinline__ void pair_force(const StepConsts& c, Lane& L, float c
         const float e2 = __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
         inter = __fadd_rn(e2, 0.0001f) < (kUniformR ? c.thr_uniform : tb.thr[pair]);
     }
-    if (inter) {
-        L.count++;
-        const float s = d2 + 0.0001f;
-        const float rs = rsqrtf(s);
-        const float r = s * rs * (kUniformR ? c.inv_eff_uniform : tb.inv_eff[pair]);
-        const float ex = __expf(c.neg_k * r * r);
-        const float net = fmaf(c.repulsion, ex, -c.attraction * r) * tb.force[L.tp * tb.T + other];
-        const float wgt = net * rs;
-        L.fx = fmaf(dx, wgt, L.fx);
-        L.fy = fmaf(dy, wgt, L.fy);
-        L.fz = fmaf(dz, wgt, L.fz);
-    }
+    return inter;
+}
+
+// The force weight of an interacting pair (multiplies the displacement).
+template <bool kUniformR>
+__device__ __forceinline__ float pair_weight(float d2, uint32_t meta, const Lane& L, const Tables& tb, float c1u)
+{
+    const uint32_t other = meta >> kTypeShift;
+    const float2 k = tb.coef[L.tp * tb.T + other];
+    const float s = d2 + 0.0001f;
+    const float rs = rsqrtf(s);
+    const float c1 = kUniformR ? c1u : tb.c1[L.tp * kTableStride + other];
+    float e;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(c1 * s));
+    return rs * fmaf(k.x, e, -k.y * (s * rs));
+}
+
+// The staged coordinates of a slot.
+__device__ __forceinline__ void staged_xyz(const float* xyf, const float* zzf, int slot, float& x, float& y, float& z)
+{
+    const int pb = (slot >> 1) * 4 + (slot & 1);
+    x = xyf[pb];
+    y = xyf[pb + 2];
+    z = zzf[slot];
 }
 
 template <int kStage, int kMinBlocks, bool kGeneric, bool kUniformR>
@@ -161,6 +180,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                       float4* __restrict__ acc, int* __restrict__ counts)
 {
     __shared__ float s_inv_eff[kUniformR ? 1 : kTableSize];
+    __shared__ float s_c1[kUniformR ? 1 : kTableSize];
     __shared__ float s_thr[kUniformR ? 1 : kTableSize];
     __shared__ float s_thr_lo[kUniformR ? 1 : kTableSize];
     extern __shared__ __align__(16) unsigned char s_dyn[];
@@ -169,18 +189,21 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         for (int e = threadIdx.x; e < T * T; e += kThreads) {
             const int a = e / T, b = e - a * T;
             const int k = a * kTableStride + b;
-            s_inv_eff[k] = 1.0f / tables->eff[k];
+            const float inv = 1.0f / tables->eff[k];
+            s_inv_eff[k] = inv;
+            s_c1[k] = c.neg_k * kLog2e * inv * inv;
             s_thr[k] = tables->threshold[k];
             s_thr_lo[k] = tables->threshold_lo[k];
         }
     }
     __syncthreads();
+    const float c1u = c.neg_k * kLog2e * c.inv_eff_uniform * c.inv_eff_uniform;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int item = blockIdx.x * kWarps + warp;
     if (item >= *n_items) return;
     WarpSmem<kStage>& w = reinterpret_cast<WarpSmem<kStage>*>(s_dyn)[warp];
-    float* wforce = reinterpret_cast<float*>(s_dyn + sizeof(WarpSmem<kStage>) * kWarps) + warp * T * T;
+    float2* wcoef = reinterpret_cast<float2*>(s_dyn + sizeof(WarpSmem<kStage>) * kWarps) + warp * T * T;
     const float* xyf = reinterpret_cast<const float*>(w.xy);
     const float* zzf = reinterpret_cast<const float*>(w.zz);
     const int2 it = items[item];
@@ -204,13 +227,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const int yc = (int)((local_first / (uint32_t)mx) % (uint32_t)my);
     const int zc = (int)(local_first / (uint32_t)(mx * my));
     const int hx = (int)((keys_sorted[t] - world_base) % (uint32_t)mx);
-    // the world's force table, compact T-stride
+    // the world's force coefficients, compact T-stride
     for (int e = lane; e < T * T; e += 32) {
         const int a = e / T, b = e - a * T;
-        wforce[e] = c.world_force[(size_t)world * kTableSize + a * kTableStride + b];
+        const float F = c.world_force[(size_t)world * kTableSize + a * kTableStride + b];
+        const float inv = kUniformR ? c.inv_eff_uniform : s_inv_eff[a * kTableStride + b];
+        wcoef[e] = make_float2(c.repulsion * F, c.attraction * F * inv);
     }
     __syncwarp();
-    const Tables tb{wforce, s_inv_eff, s_thr, s_thr_lo, T};
+    const Tables tb{wcoef, s_c1, s_thr, s_thr_lo, T};
     // x sub-ranges whose union (range plus one cell each side) fits in the box
     const int width = kGeneric ? mx : (mx - 2);
     const int passes = kGeneric ? 1 : (x1 - x0 + width) / width;
@@ -343,7 +368,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 }
             }
 
-            // ---- drain: every set bit of this lane
+            // ---- drain: every set bit of this lane, in slot order
             int gi = 0;
             uint32_t m = w.mask[lane];
             while (true) {
@@ -357,9 +382,16 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     const int slot = gi * 32 + (__ffs(m) - 1);
                     m &= m - 1u;
                     if (slot != own) {
-                        const int pb = (slot >> 1) * 4 + (slot & 1);
-                        pair_force<kGeneric, kUniformR>(c, L, xyf[pb], xyf[pb + 2], zzf[slot], w.meta[slot],
-                                                        pos_sorted, tb);
+                        float x, y, z, dx, dy, dz, d2;
+                        staged_xyz(xyf, zzf, slot, x, y, z);
+                        const uint32_t meta = w.meta[slot];
+                        if (pair_test<kGeneric, kUniformR>(c, L, x, y, z, meta, pos_sorted, tb, dx, dy, dz, d2)) {
+                            const float wgt = pair_weight<kUniformR>(d2, meta, L, tb, c1u);
+                            L.count++;
+                            L.fx = fmaf(dx, wgt, L.fx);
+                            L.fy = fmaf(dy, wgt, L.fy);
+                            L.fz = fmaf(dz, wgt, L.fz);
+                        }
                     }
                 }
             }
@@ -430,7 +462,7 @@ template <int S, int B, bool G, bool U>
 cudaError_t configure_one()
 {
     return cudaFuncSetAttribute(step_force_kernel<S, B, G, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)((sizeof(WarpSmem<S>) + sizeof(float) * kTableSize) * kWarps));
+                                (int)((sizeof(WarpSmem<S>) + sizeof(float2) * kTableSize) * kWarps));
 }
 
 template <int S, int B>
@@ -451,7 +483,7 @@ cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const 
                            const int2* items, const int* n_items, int blocks, float4* pos, float4* vel, float4* acc,
                            int* counts, cudaStream_t st)
 {
-    const size_t smem = (sizeof(WarpSmem<S>) + sizeof(float) * c.num_types * c.num_types) * kWarps;
+    const size_t smem = (sizeof(WarpSmem<S>) + sizeof(float2) * c.num_types * c.num_types) * kWarps;
 #define CF_FORCE_LAUNCH(G, U)                                                                                        \
     step_force_kernel<S, B, G, U><<<blocks, kThreads, smem, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted,   \
                                                                   cell_off, items, n_items, pos, vel, acc, counts)
