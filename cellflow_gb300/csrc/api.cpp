@@ -364,7 +364,10 @@ float filter_bound(float thr_max, float max_extent)
     std::frexp(2.0 * (double)max_extent, &ex);
     const double delta = 2.0 * std::ldexp(1.0, ex - 24);  // 2 ulp of 2 * extent
     const double bound = (b + 3.47 * delta * std::sqrt(b) + 3.0 * delta * delta) * (1.0 + 0x1p-21);
-    return nextafterf((float)bound, INFINITY);
+    // The kernel evaluates fma(dz, dz, fma(dy, dy, fma(dx, dx, -bound'))) < 0 and
+    // takes its sign bit: three roundings of magnitude <= 2^-24 max(d^2, bound')
+    // each, so bound' = bound (1 + 2^-19) keeps every pair below bound negative.
+    return nextafterf((float)(bound * (1.0 + 0x1p-19)), INFINITY);
 }
 
 int prepare_step(cf_world* w, const cf_step_params* p, StepConsts* c)
@@ -1017,7 +1020,7 @@ int cf_set_force_variant(cf_world* w, int variant)
 {
     int rc = check_world(w);
     if (rc) return rc;
-    if (variant < 0 || variant >= CF_FORCE_VARIANTS) return fail(CF_ERR_INVALID, "force variant must be 0, 1 or 2");
+    if (variant < 0 || variant >= CF_FORCE_VARIANTS) return fail(CF_ERR_INVALID, "force variant must be in [0, 4)");
     w->force_variant = variant;
     return CF_OK;
 }

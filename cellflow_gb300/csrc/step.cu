@@ -348,21 +348,24 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 }
             } else {
                 const float2 nhx = make_float2(-hxf, -hxf), nhy = make_float2(-hyf, -hyf),
-                             nhz = make_float2(-hzf, -hzf);
+                             nhz = make_float2(-hzf, -hzf), nthr = make_float2(-thr_f, -thr_f);
                 for (int gi = 0; gi < ngroups; gi++) {
+                    // d^2 - bound with the bound folded into the first FMA; the sign bit of
+                    // each result is shifted into the mask (last pair first, so pair p lands on
+                    // bits 2p, 2p + 1)
                     uint32_t m = 0;
 #pragma unroll
-                    for (int p = 0; p < 16; p++) {
+                    for (int p = 15; p >= 0; p--) {
                         const float4 a = w.xy[gi * 16 + p];
                         const float2 b = w.zz[gi * 16 + p];
                         const float2 dx = __fadd2_rn(make_float2(a.x, a.y), nhx);
                         const float2 dy = __fadd2_rn(make_float2(a.z, a.w), nhy);
                         const float2 dz = __fadd2_rn(b, nhz);
-                        float2 d2 = __fmul2_rn(dx, dx);
-                        d2 = __ffma2_rn(dy, dy, d2);
-                        d2 = __ffma2_rn(dz, dz, d2);
-                        if (d2.x < thr_f) m |= 1u << (2 * p);
-                        if (d2.y < thr_f) m |= 1u << (2 * p + 1);
+                        float2 q = __ffma2_rn(dx, dx, nthr);
+                        q = __ffma2_rn(dy, dy, q);
+                        q = __ffma2_rn(dz, dz, q);
+                        m = __funnelshift_l(__float_as_uint(q.y), m, 1);
+                        m = __funnelshift_l(__float_as_uint(q.x), m, 1);
                     }
                     w.mask[gi * 32 + lane] = m;
                 }
@@ -523,6 +526,7 @@ cudaError_t configure_step_force()
     cudaError_t e = configure_variant<256, 8>();
     if (e == cudaSuccess) e = configure_variant<256, 6>();
     if (e == cudaSuccess) e = configure_variant<512, 4>();
+    if (e == cudaSuccess) e = configure_variant<384, 6>();
     return e;
 }
 
@@ -539,6 +543,9 @@ cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, con
                                       blocks, pos, vel, acc, counts, st);
     case 2:
         return launch_variant<512, 4>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+                                      blocks, pos, vel, acc, counts, st);
+    case 3:
+        return launch_variant<384, 6>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
                                       blocks, pos, vel, acc, counts, st);
     default:
         return launch_variant<256, 8>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,

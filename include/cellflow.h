@@ -182,8 +182,9 @@ float cf_lfo_ratio(float ratio, float lfo_a, float lfo_s, float t_seconds);
 int cf_step(cf_world* w, const cf_step_params* p, int nsteps);
 /* Force-kernel variants: 0 = 256 candidates staged per warp batch, register
  * budget for 8 blocks per SM; 1 = 256 staged, 6 blocks per SM; 2 = 512
- * staged, 4 blocks per SM.  Results are bit-identical across variants. */
-#define CF_FORCE_VARIANTS 3
+ * staged, 4 blocks per SM; 3 = 384 staged, 6 blocks per SM.  Results are
+ * bit-identical across variants. */
+#define CF_FORCE_VARIANTS 4
 /* Autotuner of the step (no counterpart in the reference): runs `steps`
  * trial steps with each force-kernel variant, restores the particle state,
  * keeps the fastest variant for later steps and returns it in
