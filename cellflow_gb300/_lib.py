@@ -108,6 +108,37 @@ class PhaseTimes(C.Structure):
     ]
 
 
+class Preset(C.Structure):
+    """cf_preset: a parsed preset file (CellFlowWidget.cpp:1070-1259)."""
+
+    _fields_ = [
+        ("present", C.c_uint),
+        ("particle_count", C.c_int),
+        ("params", StepParams),
+        ("force_range", C.c_float),
+        ("force_bias", C.c_float),
+        ("force_offset", C.c_float),
+        ("ratio", C.c_float),
+        ("lfo_a", C.c_float),
+        ("lfo_s", C.c_float),
+        ("spawn_region", C.c_float),
+        ("n_radio", C.c_int),
+        ("radio", C.c_float * CF_MAX_TYPES),
+        ("n_raw", C.c_int),
+        ("raw", C.c_float * (CF_MAX_TYPES * CF_MAX_TYPES)),
+        ("n_colors", C.c_int),
+        ("colors", Color * CF_MAX_TYPES),
+        ("extra", C.c_char * 8192),
+    ]
+
+
+PRESET_BITS = {
+    "PARTICLE_COUNT": 1 << 0, "numParticleTypes": 1 << 1, "radius": 1 << 2, "delta_t": 1 << 3,
+    "friction": 1 << 4, "repulsion": 1 << 5, "attraction": 1 << 6, "k": 1 << 7, "balance": 1 << 8,
+    "forceMultiplier": 1 << 9, "canvas": 1 << 10, "forceTransform": 1 << 11, "lfo": 1 << 12,
+    "spawnRegionSize": 1 << 13, "radioByType": 1 << 14, "rawForceTable": 1 << 15, "particleColors": 1 << 16,
+}
+
 _W = C.c_void_p
 _P = C.POINTER
 _SIGNATURES = {
@@ -180,6 +211,9 @@ _SIGNATURES = {
                                       C.c_void_p]),
     "cf_rdf": (C.c_int, [_W, C.c_void_p, C.c_int, C.c_float, C.c_void_p]),
     "cf_rdf_backward": (C.c_int, [_W, C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_void_p]),
+    "cf_preset_parse": (C.c_int, [C.c_char_p, C.c_size_t, _P(Preset)]),
+    "cf_preset_apply": (C.c_int, [_W, _P(Preset), C.c_uint64, _P(StepParams)]),
+    "cf_preset_write": (C.c_int, [_W, _P(Preset), C.c_char_p, C.c_size_t, _P(C.c_size_t)]),
     "cf_profile_enable": (C.c_int, [_W, C.c_int]),
     "cf_profile_read": (C.c_int, [_W, _P(PhaseTimes)]),
     "cf_measure_fp32_peak": (C.c_int, [_P(C.c_double)]),

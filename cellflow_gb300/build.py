@@ -22,7 +22,8 @@ LIB = PKG / "libcellflow.so"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cpp", "celllist.cu", "step.cu", "proximity.cu", "init.cu", "peak.cu", "noalloc.cu", "adjoint.cu"]
+SOURCES = ["api.cpp", "celllist.cu", "step.cu", "proximity.cu", "init.cu", "peak.cu", "noalloc.cu", "adjoint.cu",
+           "preset.cpp"]
 
 
 def nvcc() -> str:

@@ -14,7 +14,7 @@ from dataclasses import dataclass, fields
 import numpy as np
 
 from . import _lib
-from ._lib import Color, DeviceView, GridInfo, Particle, StepParams, check, load
+from ._lib import Color, DeviceView, GridInfo, Particle, Preset, StepParams, check, load
 
 PARTICLE_DTYPE = np.dtype(
     [("pos", "<f4", 3), ("vel", "<f4", 3), ("acc", "<f4", 3), ("ptype", "<u4"), ("pad", "<f4")]
@@ -245,6 +245,36 @@ class ParticleSimulation:
         check(self._lib.cf_work_counters(self._h, C.byref(p), C.byref(c27), C.byref(inter)), "cf_work_counters")
         return c27.value, inter.value
 
+    # ---- presets ---------------------------------------------------------------------
+    def loadPreset(self, source, seed: int = 1, params: SimulationParams | None = None):
+        """CellFlowWidget::loadPreset (CellFlowWidget.cpp:1070-1180) on this world.  source is a path or
+        the JSON text.  Returns (SimulationParams with the preset's values, the parsed Preset)."""
+        from pathlib import Path
+
+        text = str(source).encode() if str(source).lstrip().startswith("{") else Path(source).read_bytes()
+        pre = parse_preset(text)
+        p = (params or SimulationParams()).to_c()
+        check(self._lib.cf_preset_apply(self._h, C.byref(pre), seed, C.byref(p)), "cf_preset_apply")
+        return params_from_c(p), pre
+
+    def savePreset(self, params: SimulationParams, preset: Preset | None = None, path=None) -> str:
+        """CellFlowWidget::savePreset (CellFlowWidget.cpp:1182-1259): the JSON text (written to path if
+        given); step parameters from params, transform / LFO / colours / other keys from preset."""
+        pre = Preset() if preset is None else preset
+        if preset is None:
+            pre.force_range, pre.force_bias, pre.force_offset, pre.lfo_s = 0.28, -0.20, 1.0, 0.1
+        pre.params = params.to_c()
+        n = C.c_size_t()
+        check(self._lib.cf_preset_write(self._h, C.byref(pre), None, 0, C.byref(n)), "cf_preset_write")
+        buf = C.create_string_buffer(n.value + 1)
+        check(self._lib.cf_preset_write(self._h, C.byref(pre), buf, n.value + 1, C.byref(n)), "cf_preset_write")
+        text = buf.value.decode()
+        if path is not None:
+            from pathlib import Path
+
+            Path(path).write_text(text)
+        return text
+
     # ---- differentiable rollout (device pointers, n float4 each) -------------------
     def rollout_forward(self, params: SimulationParams, steps: int, checkpoint_every: int = 16,
                         pos4_in: int | None = None, vel4_in: int | None = None, pos4_out: int | None = None,
@@ -384,6 +414,18 @@ class Batch:
 
     def sync(self) -> None:
         check(self._lib.cf_batch_sync(self._h), "cf_batch_sync")
+
+
+def parse_preset(text: str | bytes) -> Preset:
+    """cf_preset_parse: a preset file's JSON text (CellFlowWidget.cpp:1070-1180 keys)."""
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    out = Preset()
+    check(load().cf_preset_parse(data, len(data), C.byref(out)), "cf_preset_parse")
+    return out
+
+
+def params_from_c(p: StepParams) -> SimulationParams:
+    return SimulationParams(**{f.name: getattr(p, f.name) for f in fields(SimulationParams)})
 
 
 def lfo_ratio(ratio: float, lfo_a: float, lfo_s: float, t: float) -> float:

@@ -327,6 +327,64 @@ int cf_rdf(cf_world* w, const float* d_pos4, int bins, float r_max, float* d_his
 /* dL/dpos (device, n float4) of L(hist) given d_ghist = dL/dhist (device). */
 int cf_rdf_backward(cf_world* w, const float* d_pos4, int bins, float r_max, const float* d_ghist, float* d_gpos4);
 
+/* ---- presets ----------------------------------------------------------------
+ *
+ * The reference's preset files (CellFlowWidget::loadPreset / savePreset,
+ * cuda-native/src/CellFlowWidget.cpp:1070-1259): one JSON object with the
+ * reference's keys.  Keys this library does not interpret (rendering,
+ * camera, effect) are kept as JSON text and written back unchanged. */
+#define CF_PRESET_PARTICLE_COUNT (1u << 0)   /* PARTICLE_COUNT                         */
+#define CF_PRESET_NUM_TYPES (1u << 1)        /* numParticleTypes                       */
+#define CF_PRESET_RADIUS (1u << 2)           /* radius                                 */
+#define CF_PRESET_DELTA_T (1u << 3)          /* delta_t                                */
+#define CF_PRESET_FRICTION (1u << 4)         /* friction                               */
+#define CF_PRESET_REPULSION (1u << 5)        /* repulsion                              */
+#define CF_PRESET_ATTRACTION (1u << 6)       /* attraction                             */
+#define CF_PRESET_K (1u << 7)                /* k                                      */
+#define CF_PRESET_BALANCE (1u << 8)          /* balance                                */
+#define CF_PRESET_FORCE_MULTIPLIER (1u << 9) /* forceMultiplier                        */
+#define CF_PRESET_CANVAS (1u << 10)          /* canvasWidth / canvasHeight / canvasDepth */
+#define CF_PRESET_FORCE_TRANSFORM (1u << 11) /* forceRange / forceBias / forceOffset   */
+#define CF_PRESET_LFO (1u << 12)             /* ratio / lfoA / lfoS                    */
+#define CF_PRESET_SPAWN_REGION (1u << 13)    /* spawnRegionSize                        */
+#define CF_PRESET_RADIO (1u << 14)           /* radioByType                            */
+#define CF_PRESET_RAW_TABLE (1u << 15)       /* rawForceTable                          */
+#define CF_PRESET_COLORS (1u << 16)          /* particleColors                         */
+
+typedef struct cf_preset {
+    unsigned present;         /* CF_PRESET_* bits of the keys found                 */
+    int particle_count;       /* PARTICLE_COUNT                                      */
+    cf_step_params params;    /* SimulationParams defaults where a key is absent;
+                               * num_particle_types = numParticleTypes               */
+    float force_range, force_bias, force_offset; /* defaults 0.28, -0.20, 1.0      */
+    float ratio, lfo_a, lfo_s;                   /* defaults 0, 0, 0.1             */
+    float spawn_region;       /* spawnRegionSize                                     */
+    int n_radio;              /* radioByType                                         */
+    float radio[CF_MAX_TYPES];
+    int n_raw;                /* rawForceTable, row-major [self*T + other]           */
+    float raw[CF_MAX_TYPES * CF_MAX_TYPES];
+    int n_colors;             /* particleColors                                      */
+    cf_color colors[CF_MAX_TYPES];
+    char extra[8192];         /* uninterpreted keys, as JSON members                 */
+} cf_preset;
+
+/* Parse preset JSON text (UTF-8, len bytes).  Numbers as QJsonValue::toDouble
+ * reads them, narrowed to float as the reference's float fields hold them;
+ * malformed JSON returns CF_ERR_INVALID with the offset in cf_last_error(). */
+int cf_preset_parse(const char* json, size_t len, cf_preset* out);
+/* loadPreset (CellFlowWidget.cpp:1070-1180) on a world: the particle count
+ * and the type count (each respawns from seed), the radius values for
+ * i < min(len, T), the raw table for i < min(len, T*T), then
+ * cf_update_force_table(force_range, force_bias, force_offset).  The step
+ * parameters present in the preset are written into *params (others kept),
+ * params->num_particle_types = T. */
+int cf_preset_apply(cf_world* w, const cf_preset* p, uint64_t seed, cf_step_params* params);
+/* savePreset (CellFlowWidget.cpp:1182-1259): JSON text with the reference's
+ * keys, the count, types, radius values and raw table from the world and the
+ * rest from *p.  buf NULL: only the length (without the terminating NUL) in
+ * *len; otherwise cap must exceed it. */
+int cf_preset_write(cf_world* w, const cf_preset* p, char* buf, size_t cap, size_t* len);
+
 /* ---- measurement ---------------------------------------------------------- */
 
 /* Device time of the step's phases, accumulated over the steps run since
