@@ -185,6 +185,11 @@ _SIGNATURES = {
         C.c_int,
         [_W, C.c_float, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, _P(C.c_int)],
     ),
+    "cf_triangle_mesh": (C.c_int, [_W, C.c_float, C.c_int, C.c_void_p, C.c_int, _P(C.c_int)]),
+    "cf_triangle_mesh_device": (
+        C.c_int,
+        [_W, C.c_float, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, _P(C.c_int)],
+    ),
     "cf_proximity_edges_noalloc": (
         C.c_int,
         [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p, C.c_int,

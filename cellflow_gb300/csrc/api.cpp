@@ -136,6 +136,8 @@ void free_particles(cf_world* w)
     dev_free(s.cell_end);
     dev_free(s.prox_slots);
     dev_free(s.prox_count);
+    dev_free(s.mesh_slots);
+    dev_free(s.mesh_count);
     dev_free(s.counters);
     dev_free(s.cell_pop);
     dev_free(s.row_count);
@@ -237,6 +239,15 @@ int ensure_prox(cf_world* w)
     if (s.prox_slots) return CF_OK;
     CF_CUDA(dev_alloc(&s.prox_slots, (size_t)w->n * CF_MAX_PROX_CONN));
     CF_CUDA(dev_alloc(&s.prox_count, (size_t)w->n + 1));
+    return CF_OK;
+}
+
+int ensure_mesh(cf_world* w)
+{
+    Scratch& s = w->s;
+    if (s.mesh_slots) return CF_OK;
+    CF_CUDA(dev_alloc(&s.mesh_slots, (size_t)w->n * CF_MESH_MAX_CONN));
+    CF_CUDA(dev_alloc(&s.mesh_count, (size_t)w->n + 1));
     return CF_OK;
 }
 
@@ -1244,7 +1255,87 @@ int proximity_prepare(cf_world* w, float distance, int max_conn, uint32_t* total
     return sync_and_check(w);
 }
 
+// Triangle selection: cell list on the proximity grid of the mesh distance,
+// per-particle triangle counts, exclusive scan.  Leaves offsets in
+// mesh_count[0..n] and the triangle total in *total.
+int mesh_prepare(cf_world* w, float distance, int max_conn, uint32_t* total)
+{
+    if (!(distance >= 0.0f) || !std::isfinite(distance)) return fail(CF_ERR_INVALID, "distance must be finite, >= 0");
+    if (max_conn < 0) return fail(CF_ERR_INVALID, "max_conn must be >= 0");
+    if (w->worlds > 1) return fail(CF_ERR_INVALID, "the triangle mesh covers a single world");
+    int rc = ensure_mesh(w);
+    if (rc) return rc;
+    // ParticleSimulation.cu:723-724: 20 % hysteresis on the distance
+    const float hysteresis = 1.2f;
+    const float dsq = distance * distance * (hysteresis * hysteresis);
+    Grid g = choose_prox_grid(w->ext, nextafterf(std::sqrt(dsq), INFINITY), kMaxCells);
+    int which = 0;
+    rc = build_cell_list(w, g, w->ext, &which);
+    if (rc) return rc;
+    Scratch& s = w->s;
+    CF_CUDA(cudaMemsetAsync(s.mesh_count + w->n, 0, sizeof(uint32_t), w->stream));
+    CF_CUDA(launch_mesh_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_start, s.cell_end, g, w->n, dsq,
+                               std::min(max_conn, CF_MESH_MAX_CONN), s.mesh_slots, s.mesh_count, w->stream));
+    CF_CUDA(launch_scan_exclusive(s.mesh_count, s.mesh_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
+    CF_CUDA(cudaMemcpyAsync(total, s.mesh_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    return sync_and_check(w);
+}
+
 }  // namespace
+
+int cf_triangle_mesh(cf_world* w, float distance, int max_conn, int32_t* triangles, int cap, int* n_triangles)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (cap < 0 || (cap > 0 && !triangles)) return fail(CF_ERR_INVALID, "bad triangle buffer");
+    uint32_t total = 0;
+    rc = mesh_prepare(w, distance, max_conn, &total);
+    if (rc) return rc;
+    if (n_triangles) *n_triangles = (int)total;
+    const int write = (int)std::min<uint32_t>(total, (uint32_t)cap);
+    if (write > 0) {
+        int32_t* d_tris = nullptr;
+        CF_CUDA(dev_alloc(&d_tris, 3 * (size_t)write));
+        cudaError_t e = launch_mesh_emit(w->s.mesh_slots, w->s.mesh_count, w->n, w->pos, nullptr, 1, d_tris, nullptr,
+                                         write, w->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(triangles, d_tris, 12 * (size_t)write, cudaMemcpyDeviceToHost, w->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
+        cudaFree(d_tris);
+        if (e != cudaSuccess) return cuda_fail(e, "triangle mesh");
+    }
+    if (total > (uint32_t)cap) return fail(CF_ERR_CAPACITY, "triangle buffer smaller than the triangle count");
+    return CF_OK;
+}
+
+int cf_triangle_mesh_device(cf_world* w, float distance, int max_conn, const cf_color* colors, int n_colors,
+                            float* vertices, int cap_vertices, int* vertex_count)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!colors || n_colors < w->num_types) return fail(CF_ERR_INVALID, "need one colour per type");
+    if (cap_vertices < 0 || (cap_vertices > 0 && !vertices)) return fail(CF_ERR_INVALID, "bad vertex buffer");
+    uint32_t total = 0;
+    rc = mesh_prepare(w, distance, max_conn, &total);
+    if (rc) return rc;
+    if (vertex_count) *vertex_count = (int)(3 * total);
+    const long long write = std::min<long long>(total, cap_vertices / 3);
+    if (write > 0) {
+        float* d_colors = nullptr;
+        CF_CUDA(dev_alloc(&d_colors, 3 * (size_t)w->num_types));
+        // ParticleSimulation.cu:356 indexes colours by type % numParticleTypes
+        cudaError_t e = cudaMemcpyAsync(d_colors, colors, sizeof(float) * 3 * w->num_types, cudaMemcpyHostToDevice,
+                                        w->stream);
+        if (e == cudaSuccess)
+            e = launch_mesh_emit(w->s.mesh_slots, w->s.mesh_count, w->n, w->pos, d_colors, w->num_types, nullptr,
+                                 vertices, write, w->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
+        cudaFree(d_colors);
+        if (e != cudaSuccess) return cuda_fail(e, "triangle mesh vertices");
+    }
+    if (3 * (size_t)total > (size_t)cap_vertices) return fail(CF_ERR_CAPACITY, "vertex buffer too small");
+    return CF_OK;
+}
 
 int cf_proximity_edges(cf_world* w, float distance, int max_conn, int32_t* edges, int cap, int* n_edges)
 {

@@ -90,6 +90,9 @@ struct Scratch {
     // proximity
     int32_t* prox_slots = nullptr;  // n * CF_MAX_PROX_CONN partner indices
     uint32_t* prox_count = nullptr; // n + 1 (exclusive-scanned in place)
+    // triangle mesh
+    int32_t* mesh_slots = nullptr;  // n * CF_MESH_MAX_CONN neighbour indices (-1 ends a short list)
+    uint32_t* mesh_count = nullptr; // n + 1 triangles per particle, exclusive-scanned in place
     uint32_t* scan_tmp = nullptr;   // block partials of the device-wide scan
     size_t scan_tmp_cap = 0;
     // work counters
@@ -252,6 +255,12 @@ cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* ke
                                     const uint32_t* vals_sorted, const uint32_t* cell_start,
                                     const uint32_t* cell_end, const Grid& g, int n, float dsq, int max_conn,
                                     int32_t* slots, uint32_t* count, cudaStream_t st);
+cudaError_t launch_mesh_select(const float4* pos_sorted, const uint32_t* keys_sorted, const uint32_t* vals_sorted,
+                               const uint32_t* cell_start, const uint32_t* cell_end, const Grid& g, int n, float dsq,
+                               int max_conn, int32_t* slots, uint32_t* count, cudaStream_t st);
+cudaError_t launch_mesh_emit(const int32_t* slots, const uint32_t* offsets, int n, const float4* pos,
+                             const float* colors, int n_colors, int32_t* tris, float* vertices, long long cap_tris,
+                             cudaStream_t st);
 cudaError_t launch_proximity_emit_edges(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,
                                         int32_t* edges, int cap, cudaStream_t st);
 cudaError_t launch_proximity_emit_vertices(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,

@@ -134,7 +134,165 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// ---- triangle mesh (ParticleSimulation.cu:280-424) ----------------------------
+//
+// The reference scans j != i in index order and keeps the first
+// min(maxConn, 32) same-type particles with non-periodic squared distance
+// below distance^2 * 1.2^2 (the host wrapper's hysteresis, :723-724); every
+// pair of them whose indices both exceed i is a triangle (i, a, b), at most 64
+// per particle, in pair order (:333-349).  Here each particle keeps the
+// min(maxConn, 32) smallest qualifying indices over the cells within range
+// (the same list), counts its triangles, and an exclusive scan places them:
+// output in i order, then pair order.
+
+constexpr int kMeshHeld = CF_MESH_MAX_CONN;
+constexpr int kMeshMaxTriangles = 64;
+
+__global__ void __launch_bounds__(kThreads)
+    mesh_select_kernel(const float4* __restrict__ pos_sorted, const uint32_t* __restrict__ keys_sorted,
+                       const uint32_t* __restrict__ vals_sorted, const uint32_t* __restrict__ cell_start,
+                       const uint32_t* __restrict__ cell_end, Grid g, int n, float dsq, int max_conn,
+                       int32_t* __restrict__ slots, uint32_t* __restrict__ count)
+{
+    const int t = blockIdx.x * kThreads + threadIdx.x;
+    if (t >= n) return;
+    const float4 h = pos_sorted[t];
+    const uint32_t i = vals_sorted[t];
+    const uint32_t key = keys_sorted[t];
+    const int mx = g.m[0], my = g.m[1], mz = g.m[2];
+    const int cx = (int)(key % (uint32_t)mx);
+    const int cy = (int)((key / (uint32_t)mx) % (uint32_t)my);
+    const int cz = (int)(key / (uint32_t)(mx * my));
+    const int cap = min(max_conn, kMeshHeld);
+    int held = 0;
+    int hj[kMeshHeld];
+    if (cap > 0) {
+        for (int z = max(cz - 1, 0); z <= min(cz + 1, mz - 1); z++)
+            for (int y = max(cy - 1, 0); y <= min(cy + 1, my - 1); y++)
+                for (int x = max(cx - 1, 0); x <= min(cx + 1, mx - 1); x++) {
+                    const uint32_t cell = (uint32_t)((z * my + y) * mx + x);
+                    const uint32_t u_end = cell_end[cell];
+                    for (uint32_t u = cell_start[cell]; u < u_end; u++) {
+                        const float4 q = pos_sorted[u];
+                        if (__float_as_uint(q.w) != __float_as_uint(h.w)) continue;
+                        const int j = (int)vals_sorted[u];
+                        if (j == (int)i) continue;
+                        if (held == cap && j >= hj[cap - 1]) continue;
+                        // ParticleSimulation.cu:314-317, rounded on its own in source order
+                        const float dx = __fsub_rn(q.x, h.x);
+                        const float dy = __fsub_rn(q.y, h.y);
+                        const float dz = __fsub_rn(q.z, h.z);
+                        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                        if (!(d2 < dsq)) continue;
+                        int p = held < cap ? held : cap - 1;
+                        while (p > 0 && hj[p - 1] > j) {
+                            hj[p] = hj[p - 1];
+                            p--;
+                        }
+                        hj[p] = j;
+                        if (held < cap) held++;
+                    }
+                }
+    }
+    // the held list is in index order: the ones above i form its tail
+    int above = 0;
+    for (int e = 0; e < held; e++) {
+        slots[(size_t)i * kMeshHeld + e] = hj[e];
+        above += hj[e] > (int)i ? 1 : 0;
+    }
+    if (held < kMeshHeld) slots[(size_t)i * kMeshHeld + held] = -1;
+    count[i] = (uint32_t)min(above * (above - 1) / 2, kMeshMaxTriangles);
+}
+
+// Triangles of particle i in the reference's pair order, placed at offsets[i];
+// index triples and / or vertices of 9 floats (position, flat normal, colour).
+__global__ void __launch_bounds__(256)
+    mesh_emit_kernel(const int32_t* __restrict__ slots, const uint32_t* __restrict__ offsets, int n,
+                     const float4* __restrict__ pos, const float* __restrict__ colors, int n_colors,
+                     int32_t* __restrict__ tris, float* __restrict__ vertices, long long cap_tris)
+{
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = offsets[i], total = offsets[i + 1] - o;
+    if (total == 0) return;
+    int list[kMeshHeld];
+    int m = 0;
+    for (int e = 0; e < kMeshHeld; e++) {
+        const int j = slots[(size_t)i * kMeshHeld + e];
+        if (j < 0) break;
+        if (j > i) list[m++] = j;
+    }
+    const float4 v1 = pos[i];
+    float cr = 0.0f, cg = 0.0f, cb = 0.0f;
+    if (vertices) {  // colours are given only with a vertex buffer
+        const uint32_t c = (__float_as_uint(v1.w) & kTypeMask) % (uint32_t)n_colors;
+        cr = colors[3 * c];
+        cg = colors[3 * c + 1];
+        cb = colors[3 * c + 2];
+    }
+    uint32_t made = 0;
+    for (int a = 0; a < m && made < total; a++)
+        for (int b = a + 1; b < m && made < total; b++, made++) {
+            const long long k = (long long)o + made;
+            if (k >= cap_tris) return;
+            if (tris) {
+                tris[3 * k] = i;
+                tris[3 * k + 1] = list[a];
+                tris[3 * k + 2] = list[b];
+            }
+            if (!vertices) continue;
+            const float4 v2 = pos[list[a]], v3 = pos[list[b]];
+            // ParticleSimulation.cu:365-382, each operation rounded on its own
+            const float e1x = __fsub_rn(v2.x, v1.x), e1y = __fsub_rn(v2.y, v1.y), e1z = __fsub_rn(v2.z, v1.z);
+            const float e2x = __fsub_rn(v3.x, v1.x), e2y = __fsub_rn(v3.y, v1.y), e2z = __fsub_rn(v3.z, v1.z);
+            float nx = __fsub_rn(__fmul_rn(e1y, e2z), __fmul_rn(e1z, e2y));
+            float ny = __fsub_rn(__fmul_rn(e1z, e2x), __fmul_rn(e1x, e2z));
+            float nz = __fsub_rn(__fmul_rn(e1x, e2y), __fmul_rn(e1y, e2x));
+            const float len =
+                __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz)));
+            if (len > 0.0001f) {
+                nx = __fdiv_rn(nx, len);
+                ny = __fdiv_rn(ny, len);
+                nz = __fdiv_rn(nz, len);
+            }
+            float* v = vertices + k * 27;
+            const float4* vs[3] = {&v1, &v2, &v3};
+            for (int q = 0; q < 3; q++) {
+                v[9 * q + 0] = vs[q]->x;
+                v[9 * q + 1] = vs[q]->y;
+                v[9 * q + 2] = vs[q]->z;
+                v[9 * q + 3] = nx;
+                v[9 * q + 4] = ny;
+                v[9 * q + 5] = nz;
+                v[9 * q + 6] = cr;
+                v[9 * q + 7] = cg;
+                v[9 * q + 8] = cb;
+            }
+        }
+}
+
 }  // namespace
+
+cudaError_t launch_mesh_select(const float4* pos_sorted, const uint32_t* keys_sorted, const uint32_t* vals_sorted,
+                               const uint32_t* cell_start, const uint32_t* cell_end, const Grid& g, int n, float dsq,
+                               int max_conn, int32_t* slots, uint32_t* count, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    mesh_select_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted,
+                                                                          cell_start, cell_end, g, n, dsq, max_conn,
+                                                                          slots, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mesh_emit(const int32_t* slots, const uint32_t* offsets, int n, const float4* pos,
+                             const float* colors, int n_colors, int32_t* tris, float* vertices, long long cap_tris,
+                             cudaStream_t st)
+{
+    if (n <= 0 || cap_tris <= 0) return cudaSuccess;
+    mesh_emit_kernel<<<(n + 255) / 256, 256, 0, st>>>(slots, offsets, n, pos, colors, n_colors, tris, vertices,
+                                                      cap_tris);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* keys_sorted,
                                     const uint32_t* vals_sorted, const uint32_t* cell_start,

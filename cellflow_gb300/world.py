@@ -245,6 +245,26 @@ class ParticleSimulation:
         check(self._lib.cf_work_counters(self._h, C.byref(p), C.byref(c27), C.byref(inter)), "cf_work_counters")
         return c27.value, inter.value
 
+    # ---- triangle mesh -----------------------------------------------------------------
+    def triangle_mesh(self, distance: float, max_conn: int) -> np.ndarray:
+        """Triangles of generateTriangleMesh (ParticleSimulation.cu:689-747) as index triples, shape (K, 3)."""
+        count = C.c_int()
+        check(self._lib.cf_triangle_mesh(self._h, distance, max_conn, None, 0, C.byref(count)), "cf_triangle_mesh")
+        tris = np.zeros((max(count.value, 1), 3), dtype=np.int32)
+        check(self._lib.cf_triangle_mesh(self._h, distance, max_conn, _ptr(tris), count.value, C.byref(count)),
+              "cf_triangle_mesh")
+        return tris[: count.value].copy()
+
+    def triangle_mesh_device(self, distance: float, max_conn: int, colors, vertices_ptr: int,
+                             cap_vertices: int) -> int:
+        """The reference's 9-float triangle vertices into a device buffer; returns the vertex count."""
+        cols = (Color * len(colors))(*[Color(*c) for c in colors])
+        count = C.c_int()
+        check(self._lib.cf_triangle_mesh_device(self._h, distance, max_conn, cols, len(colors),
+                                                C.c_void_p(vertices_ptr), cap_vertices, C.byref(count)),
+              "cf_triangle_mesh_device")
+        return count.value
+
     # ---- presets ---------------------------------------------------------------------
     def loadPreset(self, source, seed: int = 1, params: SimulationParams | None = None):
         """CellFlowWidget::loadPreset (CellFlowWidget.cpp:1070-1180) on this world.  source is a path or

@@ -223,6 +223,24 @@ int cf_proximity_edges(cf_world* w, float distance, int max_conn, int32_t* edges
 int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, const cf_color* colors, int n_colors,
                                  float* vertices, int cap_vertices, int* vertex_count);
 
+/* Triangle mesh, generateTriangleMesh (ParticleSimulation.cu:689-747, kernel
+ * :280-424): for each particle i, the first min(max_conn, 32) other particles
+ * of its type in index order with non-periodic squared distance below
+ * distance^2 * 1.2^2 (the reference's hysteresis, :723-724); every pair (a, b)
+ * of them with both indices above i is a triangle (i, a, b), at most 64 per
+ * particle.  Output in i order, then pair order (the reference appended
+ * through an atomicAdd, so its order varied; the set is the same).
+ * cf_triangle_mesh writes 3 indices per triangle to host memory
+ * (CF_ERR_CAPACITY when the count exceeds cap, *n_triangles always set). */
+#define CF_MESH_MAX_CONN 32
+int cf_triangle_mesh(cf_world* w, float distance, int max_conn, int32_t* triangles, int cap, int* n_triangles);
+/* The same triangles as the reference's vertices: 3 per triangle, 9 floats
+ * each (x, y, z, flat normal, colour of i's type: colors[type % T]) into a
+ * DEVICE buffer of cap_vertices*9 floats standing in for the GL VBO;
+ * *vertex_count = 3 * triangles. */
+int cf_triangle_mesh_device(cf_world* w, float distance, int max_conn, const cf_color* colors, int n_colors,
+                            float* vertices, int cap_vertices, int* vertex_count);
+
 /* Proximity edges without allocating: the same edges, in the same order, as
  * cf_proximity_edges, for callers that may not allocate device memory while
  * they run -- a renderer's frame loop building the graph every frame (an

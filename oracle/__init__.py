@@ -70,7 +70,7 @@ def build_oracle(force: bool = False) -> Path:
 def build_ref(gpu: bool = True) -> bool:
     """Run build_ref.sh; True when oracle/_ref/libcfref.so exists afterwards."""
     inputs = [REF_DIR / "ref_step_kernel.inc", HERE / "ref_host_shim.cu", HERE / "ref_gpu_shim.cu",
-              HERE / "build_ref.sh"]
+              HERE / "build_ref.sh", REF_DIR / "ref_mesh_kernel.inc"]
     outputs = [REF_LIB] + ([REF_GPU_LIB] if gpu else [])
     ref_src = Path(os.environ.get("CELLFLOW_REFERENCE", "/root/reference")) / "cuda-native/src/ParticleSimulation.cu"
     if not ref_src.exists() and all(p.exists() for p in outputs + inputs[:1]):
@@ -109,6 +109,8 @@ def lib() -> C.CDLL:
         L.cfo_cell_list.restype = None
         L.cfo_c27.argtypes = [C.c_int, vp, vp, vp]
         L.cfo_c27.restype = C.c_double
+        L.cfo_triangle_mesh.argtypes = [C.c_int, vp, vp, C.c_float, C.c_int, vp, C.c_int, vp, vp, C.c_long]
+        L.cfo_triangle_mesh.restype = C.c_long
         P64 = C.POINTER(Phys64)
         L.cfo_rollout_f64.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, C.c_int, P64, vp, C.c_int, vp, vp]
         L.cfo_rollout_f64.restype = None
@@ -143,6 +145,8 @@ def ref_lib() -> C.CDLL:
         L.cfref_step.restype = None
         L.cfref_proximity.argtypes = [C.c_int, vp, f, C.c_int, vp, C.c_int, vp]
         L.cfref_proximity.restype = C.c_int
+        L.cfref_triangle_mesh.argtypes = [C.c_int, vp, f, C.c_int, vp, C.c_int, vp]
+        L.cfref_triangle_mesh.restype = C.c_int
         L.cfref_force_table.argtypes = [vp, C.c_int, f, f, f, vp]
         L.cfref_force_table.restype = C.c_int
         L.cfref_sizeof_particle.restype = C.c_int
@@ -237,6 +241,20 @@ def proximity_edges(pos, types, distance, max_conn) -> np.ndarray:
     return edges[:total].copy()
 
 
+def triangle_mesh(pos, types, distance, max_conn, colors, num_types):
+    """Restated triangle mesh: (triangles (K, 3) int32, vertices (3K, 9) float32), in i order."""
+    pos = _f32(pos, (-1, 3))
+    types = np.ascontiguousarray(types, dtype=np.uint32)
+    cols = _f32(colors, (-1, 3))
+    n = len(pos)
+    total = lib().cfo_triangle_mesh(n, _p(pos), _p(types), distance, max_conn, _p(cols), num_types, None, None, 0)
+    tris = np.zeros((max(total, 1), 3), dtype=np.int32)
+    verts = np.zeros((max(3 * total, 1), 9), dtype=np.float32)
+    lib().cfo_triangle_mesh(n, _p(pos), _p(types), distance, max_conn, _p(cols), num_types, _p(tris), _p(verts),
+                            total)
+    return tris[:total].copy(), verts[:3 * total].copy()
+
+
 def cell_list(pos, cells, inv_cell):
     pos = _f32(pos, (-1, 3))
     n = len(pos)
@@ -299,6 +317,17 @@ def ref_proximity_vertices(records, distance, max_conn, colors, num_types) -> np
     verts = np.zeros((max(n * 2 * mc * 2, 1), 6), dtype=np.float32)
     cols = _f32(colors, (-1, 3))
     count = ref_lib().cfref_proximity(n, _p(rec), distance, max_conn, _p(cols), num_types, _p(verts))
+    return verts[:count].copy()
+
+
+def ref_triangle_mesh(records, distance, max_conn, colors, num_types) -> np.ndarray:
+    """The reference triangle-mesh kernel body (ParticleSimulation.cu:280-424) on the host, in i order,
+    with the host wrapper's squared distance.  Returns the vertices, shape (V, 9)."""
+    rec = np.ascontiguousarray(records, dtype=PARTICLE_DTYPE)
+    n = len(rec)
+    verts = np.zeros((max(n * 64 * 3, 1), 9), dtype=np.float32)
+    cols = _f32(colors, (-1, 3))
+    count = ref_lib().cfref_triangle_mesh(n, _p(rec), distance, max_conn, _p(cols), num_types, _p(verts))
     return verts[:count].copy()
 
 

@@ -2,7 +2,7 @@
 # build_ref.sh - builds oracle/_ref/ from the reference sources, for checking.
 #
 # TEST INFRASTRUCTURE.  Where the reference tree is present (REF below), the
-# three kernel bodies are cut from it by line range after a sha256 check of
+# kernel bodies are cut from it by line range after a sha256 check of
 # the file, together with its SimulationParams.h, into oracle/_ref/ (which
 # git ignores, so no reference source enters the repository).  Whenever those
 # pieces are present, it compiles:
@@ -29,6 +29,7 @@ if [ -f "$SRC" ] && [ -f "$HDR" ]; then
     echo "$HDR_SHA  $HDR" | sha256sum -c --quiet -
     sed -n '69,166p' "$SRC" > "$OUT/ref_step_kernel.inc"
     sed -n '188,277p' "$SRC" > "$OUT/ref_prox_kernel.inc"
+    sed -n '280,424p' "$SRC" > "$OUT/ref_mesh_kernel.inc"
     sed -n '521,531p' "$SRC" > "$OUT/ref_force_table.inc"
     rm -f "$OUT/SimulationParams.h"
     cp "$HDR" "$OUT/SimulationParams.h"

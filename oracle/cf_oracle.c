@@ -23,6 +23,7 @@
  *   cfo_force_table     cuda-native/src/ParticleSimulation.cu:521-531
  *   cfo_rotate          cuda-native/src/ParticleSimulation.cu:594-605
  *   cfo_proximity_edges cuda-native/src/ParticleSimulation.cu:198-276
+ *   cfo_triangle_mesh   cuda-native/src/ParticleSimulation.cu:290-423, 723-724
  *   cfo_lfo             cuda-native/src/CellFlowWidget.cpp:414-421
  *   cfo_cell_list       no reference counterpart (the reference is O(N^2));
  *                       defines the stable cell order the GPU list must match.
@@ -390,5 +391,84 @@ double cfo_c27(int n, const float* pos, const int* m, const float* inv_cell)
     }
     free(pop);
     free(cell);
+    return total;
+}
+
+/*
+ * Triangle mesh (ParticleSimulation.cu:290-423, host wrapper :723-724).  For
+ * each i: scan j != i in index order while fewer than min(max_conn, 32) are
+ * held, keeping j of the same type with non-periodic squared distance below
+ * distance^2 * 1.2^2; every pair (a, b), a < b, of the held list whose
+ * indices both exceed i is a triangle (i, a, b), at most 64 per i, in that
+ * order.  Each triangle: 3 vertices of 9 floats (x, y, z, flat normal,
+ * colour of i's type % T).  tris gets 3 indices per triangle, verts 27 floats
+ * (either may be NULL).  Triangles beyond cap are counted, not written.
+ * Returns the triangle count.
+ */
+long cfo_triangle_mesh(int n, const float* pos, const uint32_t* type, float distance, int max_conn_in,
+                       const float* colors, int num_types, int32_t* tris, float* verts, long cap)
+{
+    const float hysteresis = 1.2f;
+    const float dsq = distance * distance * (hysteresis * hysteresis);
+    int max_conn = max_conn_in < 32 ? max_conn_in : 32;
+    long total = 0;
+    for (int i = 0; i < n; i++) {
+        int near[32];
+        int held = 0;
+        for (int j = 0; j < n && held < max_conn; j++) {
+            if (j == i || type[i] != type[j]) continue;
+            float dx = pos[3 * j] - pos[3 * i];
+            float dy = pos[3 * j + 1] - pos[3 * i + 1];
+            float dz = pos[3 * j + 2] - pos[3 * i + 2];
+            float d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 < dsq) near[held++] = j;
+        }
+        int made = 0;
+        const float* c = colors + 3 * (type[i] % (uint32_t)num_types);
+        for (int a = 0; a < held && made < 64; a++) {
+            for (int b = a + 1; b < held && made < 64; b++) {
+                int n1 = near[a], n2 = near[b];
+                if (!(i < n1 && i < n2)) continue;
+                if (total < cap) {
+                    if (tris) {
+                        tris[3 * total] = i;
+                        tris[3 * total + 1] = n1;
+                        tris[3 * total + 2] = n2;
+                    }
+                    if (verts) {
+                        const float* v1 = pos + 3 * i;
+                        const float* v2 = pos + 3 * n1;
+                        const float* v3 = pos + 3 * n2;
+                        float e1x = v2[0] - v1[0], e1y = v2[1] - v1[1], e1z = v2[2] - v1[2];
+                        float e2x = v3[0] - v1[0], e2y = v3[1] - v1[1], e2z = v3[2] - v1[2];
+                        float nx = e1y * e2z - e1z * e2y;
+                        float ny = e1z * e2x - e1x * e2z;
+                        float nz = e1x * e2y - e1y * e2x;
+                        float len = sqrtf(nx * nx + ny * ny + nz * nz);
+                        if (len > 0.0001f) {
+                            nx /= len;
+                            ny /= len;
+                            nz /= len;
+                        }
+                        const float* vs[3] = {v1, v2, v3};
+                        for (int k = 0; k < 3; k++) {
+                            float* o = verts + 27 * total + 9 * k;
+                            o[0] = vs[k][0];
+                            o[1] = vs[k][1];
+                            o[2] = vs[k][2];
+                            o[3] = nx;
+                            o[4] = ny;
+                            o[5] = nz;
+                            o[6] = c[0];
+                            o[7] = c[1];
+                            o[8] = c[2];
+                        }
+                    }
+                }
+                total++;
+                made++;
+            }
+        }
+    }
     return total;
 }

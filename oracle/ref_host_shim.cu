@@ -6,6 +6,7 @@
  * includes them unchanged:
  *   ref_step_kernel.inc  cuda-native/src/ParticleSimulation.cu:69-166
  *   ref_prox_kernel.inc  cuda-native/src/ParticleSimulation.cu:188-277
+ *   ref_mesh_kernel.inc  cuda-native/src/ParticleSimulation.cu:280-424
  *   ref_force_table.inc  cuda-native/src/ParticleSimulation.cu:521-531
  * It is compiled by nvcc as host code (as the reference's host code was, so
  * tanh(float) resolves to the float overload) with -ffp-contract=off, which
@@ -42,6 +43,7 @@ static int cfref_atomic_add(int* address, int value) { return __atomic_fetch_add
 
 #include "ref_step_kernel.inc"
 #include "ref_prox_kernel.inc"
+#include "ref_mesh_kernel.inc"
 
 #undef blockIdx
 #undef blockDim
@@ -126,6 +128,23 @@ int cfref_proximity(int n, const Particle* particles, float distance, int max_co
     for (int i = 0; i < n; i++) {
         select_particle(i);
         generateProximityGraphKernel(particles, n, dsq, max_conn, colors, num_types, vertices, &count);
+    }
+    return count;
+}
+
+/* The reference triangle-mesh kernel body for every particle, in index order,
+ * on one thread (so the triangles come in i order).  The squared distance is
+ * the host wrapper's, with its 1.2 hysteresis (ParticleSimulation.cu:723-724).
+ * `vertices` needs room for n * 64 * 3 * 9 floats.  Returns the vertex count. */
+int cfref_triangle_mesh(int n, const Particle* particles, float distance, int max_conn, const ParticleColor* colors,
+                        int num_types, float* vertices)
+{
+    int count = 0;
+    const float hysteresis = 1.2f;
+    const float dsq = distance * distance * (hysteresis * hysteresis);
+    for (int i = 0; i < n; i++) {
+        select_particle(i);
+        generateTriangleMeshKernel(particles, n, dsq, max_conn, colors, num_types, vertices, &count);
     }
     return count;
 }

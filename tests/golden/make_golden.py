@@ -132,9 +132,41 @@ def main(ref_root: str = "/root/reference") -> None:
     np.savez_compressed(HERE / "proximity_n4096.npz", **prox)
     manifest["fixtures"]["proximity_n4096.npz"] = {"n": 4096, "seed": 0x5EED0020,
                                                     "source": "reference proximity kernel body, i order"}
+    mesh_golden(manifest)
     (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1) + "\n")
     print("golden vectors written to", HERE)
 
 
+# 5. triangle mesh (reference kernel body, host wrapper's distance, i order)
+MESH_CASES = {"a": (0.15, 5, 3), "b": (0.25, 32, 2), "c": (0.31, 40, 4)}  # b and c reach 64 triangles
+
+
+def mesh_golden(manifest: dict) -> None:
+    mesh = {}
+    n = 1024
+    for tag, (dist, mc, T) in MESH_CASES.items():
+        pos = inputs.uniform_positions(n, 0x5EED0030)
+        types = inputs.uniform_types(n, T, 0x5EED0030)
+        cols = (np.arange(3 * T, dtype=np.float32).reshape(T, 3) + 1.0) / np.float32(3 * T)
+        verts = oracle.ref_triangle_mesh(oracle.to_records(pos, np.zeros_like(pos), types), dist, mc, cols, T)
+        mesh[f"{tag}_vertices"] = verts
+        mesh[f"{tag}_args"] = np.asarray([dist, mc, T], np.float64)
+    np.savez_compressed(HERE / "mesh_n1024.npz", **mesh)
+    manifest["fixtures"].pop("mesh_n2048.npz", None)
+    manifest["fixtures"]["mesh_n1024.npz"] = {"n": n, "seed": 0x5EED0030, "colors": "(arange(3T) + 1) / 3T",
+                                              "source": "reference triangle-mesh kernel body, i order"}
+
+
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) > 1 and sys.argv[-1] == "--mesh-only":
+        # add the mesh fixture to an existing manifest without rewriting the others
+        import os
+
+        os.environ["CELLFLOW_REFERENCE"] = sys.argv[1] if len(sys.argv) > 2 else "/root/reference"
+        if not oracle.build_ref(gpu=False):
+            raise SystemExit("reference pieces not found")
+        m = json.loads((HERE / "manifest.json").read_text())
+        mesh_golden(m)
+        (HERE / "manifest.json").write_text(json.dumps(m, indent=1) + "\n")
+    else:
+        main(*sys.argv[1:])

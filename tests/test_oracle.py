@@ -62,6 +62,28 @@ def test_golden_proximity():
         assert np.array_equal(edges, g[f"{tag}_edges"]), tag
 
 
+def mesh_case(g, tag, n=1024, seed=0x5EED0030):
+    dist, mc, T = g[f"{tag}_args"]
+    T = int(T)
+    pos = inputs.uniform_positions(n, seed)
+    types = inputs.uniform_types(n, T, seed)
+    cols = (np.arange(3 * T, dtype=np.float32).reshape(T, 3) + 1.0) / np.float32(3 * T)
+    return pos, types, float(dist), int(mc), cols, T
+
+
+def test_golden_triangle_mesh():
+    """The restated mesh reproduces the reference kernel body's vertices bit for bit, including the
+    64-triangle cap (case b) and max_conn above 32 (case c)."""
+    g = load("mesh_n1024.npz")
+    for tag in ("a", "b", "c"):
+        pos, types, dist, mc, cols, T = mesh_case(g, tag)
+        tris, verts = oracle.triangle_mesh(pos, types, dist, mc, cols, T)
+        assert np.array_equal(verts.view(np.uint32), g[f"{tag}_vertices"].view(np.uint32)), tag
+        assert np.all(tris[:, 0] < tris[:, 1]) and np.all(tris[:, 1] < tris[:, 2])
+    per = np.bincount(oracle.triangle_mesh(*mesh_case(g, "b"))[0][:, 0])
+    assert per.max() == 64
+
+
 def test_fp64_oracle_close_to_fp32():
     w = inputs.PLAIN_SMALL
     pos, types, table = w.positions(), w.types(), w.table()
