@@ -1304,6 +1304,7 @@ int cf_triangle_mesh(cf_world* w, float distance, int max_conn, int32_t* triangl
         cudaFree(d_tris);
         if (e != cudaSuccess) return cuda_fail(e, "triangle mesh");
     }
+    if (!triangles && cap == 0) return CF_OK;  // a count query
     if (total > (uint32_t)cap) return fail(CF_ERR_CAPACITY, "triangle buffer smaller than the triangle count");
     return CF_OK;
 }
@@ -1333,6 +1334,7 @@ int cf_triangle_mesh_device(cf_world* w, float distance, int max_conn, const cf_
         cudaFree(d_colors);
         if (e != cudaSuccess) return cuda_fail(e, "triangle mesh vertices");
     }
+    if (!vertices && cap_vertices == 0) return CF_OK;  // a count query
     if (3 * (size_t)total > (size_t)cap_vertices) return fail(CF_ERR_CAPACITY, "vertex buffer too small");
     return CF_OK;
 }

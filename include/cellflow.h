@@ -231,7 +231,9 @@ int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, cons
  * particle.  Output in i order, then pair order (the reference appended
  * through an atomicAdd, so its order varied; the set is the same).
  * cf_triangle_mesh writes 3 indices per triangle to host memory
- * (CF_ERR_CAPACITY when the count exceeds cap, *n_triangles always set). */
+ * (CF_ERR_CAPACITY when the count exceeds cap, *n_triangles always set;
+ * triangles NULL with cap 0 only counts, as does a NULL vertex buffer with
+ * cap_vertices 0 below). */
 #define CF_MESH_MAX_CONN 32
 int cf_triangle_mesh(cf_world* w, float distance, int max_conn, int32_t* triangles, int cap, int* n_triangles);
 /* The same triangles as the reference's vertices: 3 per triangle, 9 floats
