@@ -113,6 +113,25 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float) -> float:
+    """The largest value over the ranks of the process group (x itself without one).  Replicas
+    only: this timing reduction is the one collective of a multi-GPU run."""
+    import torch
+    import torch.distributed as dist
+
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return x
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, ms_max: float, world: int) -> float:
+    """Whole-job units/s of `world` replicas that each processed units_per_rank, the slowest in ms_max."""
+    return units_per_rank * world / (ms_max * 1e-3)
+
+
 def cpu_reference_sample(w, params, pos, types, table, radio, budget_s: float):
     """Times the reference step on the host over a strided sample of rows.
     Returns (particle-steps/s, kind, cores, sample description)."""
@@ -307,12 +326,8 @@ def run_gb300(args, rank, world, local):
     _lib.check(lib.cf_profile_read(sim.handle, C.byref(prof)), "cf_profile_read")
     _lib.check(lib.cf_profile_enable(sim.handle, 0), "cf_profile_enable")
     step_ms_total = prof.cell_list_ms + prof.force_ms
-    t_max = step_ms_total
-    if world > 1:
-        t = torch.tensor([step_ms_total], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = w.n * args.steps * world / (t_max * 1e-3)
+    t_max = max_over_ranks(step_ms_total)
+    value = replica_throughput(w.n * args.steps, t_max, world)
 
     # ---- work counters: replay the same K steps from the same state, untimed
     sim.set_state(*state0)
@@ -469,13 +484,9 @@ def run_batched(args, rank, world, local):
     barrier()
     clk = clocks.stop()
     batch_ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
-    t_max = batch_ms
-    if world > 1:
-        t = torch.tensor([batch_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(batch_ms)
     steps_timed = replays * bw.graph_steps
-    value = total * steps_timed * world / (t_max * 1e-3)
+    value = replica_throughput(total * steps_timed, t_max, world)
 
     # ---- end to end: host state in (pinned), one replay, host state out
     pin = lambda shape, dt: torch.empty(shape, dtype=dt).pin_memory()  # noqa: E731

@@ -123,6 +123,16 @@ public:
                                            (int)particleColors.size(), deviceVertices, capacityVertices,
                                            &outVertexCount));
     }
+    // generateTriangleMesh (ParticleSimulation.cuh:69-74) with the GL VBO
+    // replaced by a device buffer of capacityVertices * 9 floats.
+    void generateTriangleMesh(float* deviceVertices, int capacityVertices, int& outVertexCount,
+                              float proximityDistance, int maxConnectionsPerParticle,
+                              const std::vector<ParticleColor>& particleColors)
+    {
+        check(cf_triangle_mesh_device(w_, proximityDistance, maxConnectionsPerParticle, particleColors.data(),
+                                      (int)particleColors.size(), deviceVertices, capacityVertices,
+                                      &outVertexCount));
+    }
     cf_world* handle() const { return w_; }
 
 private:
