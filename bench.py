@@ -49,6 +49,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--prox-calls", type=int, default=50, help="proximity-graph calls timed (workloads with a distance)")
     return ap.parse_args()
 
 
@@ -378,6 +379,9 @@ def run_gb300(args, rank, world, local):
     # ---- reference kernel on this GPU (its O(N^2) kernel built for sm_103a), a few steps
     ref_gpu = reference_gpu_kernel(w, params, pos, types, table, radio, stream) if rank == 0 else None
 
+    # ---- proximity graph (edges/s) on the state the timed steps left
+    prox = proximity_timing(sim, w, stream, args.prox_calls) if w.prox_distance is not None else None
+
     line = None
     if rank == 0:
         cpu = None
@@ -416,6 +420,7 @@ def run_gb300(args, rank, world, local):
             "wall_s_timed_region": wall,
             "cpu_baseline": cpu,
             "reference_gpu_kernel": ref_gpu,
+            "proximity": prox,
             "library": cf.__name__ + ": " + _lib.load().cf_version().decode(),
         }
         print(json.dumps(line), flush=True)
@@ -689,6 +694,77 @@ def run_rollout(args, rank, world, local):
             "library": cf.__name__ + ": " + lib.cf_version().decode(),
         }
         print(json.dumps(line), flush=True)
+
+
+def proximity_timing(sim, w, stream, calls):
+    """Proximity-graph edges/s at the workload's distance and connection limit, in the
+    reference's call shape (generateProximityGraph, ParticleSimulation.cu:625-687): line
+    vertices written into a device buffer standing in for the GL VBO, the vertex count read
+    back, one synchronising call per frame.  Also the host edge list (cf_proximity_edges)
+    and the reference's own kernel built for sm_103a on the same particles."""
+    import numpy as np
+    import torch
+
+    import oracle
+
+    n, mc, dist = w.n, w.prox_max_conn, w.prox_distance
+    cap_v = 2 * n * mc
+    verts = torch.empty(cap_v * 6, dtype=torch.float32, device="cuda")
+    colors = [((t * 37 % 11) / 10.0, (t * 53 % 7) / 6.0, (t * 17 % 5) / 4.0) for t in range(w.num_types)]
+    torch.cuda.synchronize()
+    for _ in range(3):
+        sim.proximity_vertices_device(dist, mc, colors, verts.data_ptr(), cap_v)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        nv = sim.proximity_vertices_device(dist, mc, colors, verts.data_ptr(), cap_v)
+    dev_s = (time.perf_counter() - t0) / calls
+    edges = nv // 2
+    sim.proximity_edges(dist, mc)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        host_edges = sim.proximity_edges(dist, mc)
+    host_s = (time.perf_counter() - t0) / calls
+    out = {
+        "distance": dist, "max_conn": mc, "edges": int(edges), "calls": calls,
+        "value": edges / dev_s, "unit": "edges/s", "ms_per_call": dev_s * 1e3,
+        "path": "cf_proximity_vertices_device (device VBO, count read back; synchronising, as the reference)",
+        "host_edges": {"value": len(host_edges) / host_s, "unit": "edges/s", "ms_per_call": host_s * 1e3,
+                       "path": "cf_proximity_edges (int32 pairs into host memory)"},
+    }
+    try:
+        lib = oracle.ref_gpu_lib()
+    except (FileNotFoundError, OSError) as exc:
+        out["reference_gpu_kernel"] = {"unavailable": str(exc)}
+        return out
+    rec = sim.getParticleData()
+    parts = torch.from_numpy(np.ascontiguousarray(rec).view(np.uint8).copy()).cuda()
+    cols = torch.tensor(np.asarray(colors, np.float32).ravel(), device="cuda")
+    ref_verts = torch.empty(n * 2 * min(mc, 32) * 6, dtype=torch.float32, device="cuda")
+    count = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ref_calls = 3
+    times = []
+    with torch.cuda.stream(stream):
+        for k in range(ref_calls + 1):
+            count.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rc = lib.cfref_gpu_proximity(C.c_void_p(parts.data_ptr()), n, dist, mc, C.c_void_p(cols.data_ptr()),
+                                         w.num_types, C.c_void_p(ref_verts.data_ptr()),
+                                         C.c_void_p(count.data_ptr()), C.c_void_p(stream.cuda_stream))
+            if rc:
+                raise RuntimeError(f"reference proximity kernel launch failed: {rc}")
+            e1.record(stream)
+            e1.synchronize()
+            if k:
+                times.append(e0.elapsed_time(e1))
+    ref_edges = int(count.item()) // 2
+    ms = sum(times) / len(times)
+    out["reference_gpu_kernel"] = {
+        "value": ref_edges / (ms * 1e-3), "unit": "edges/s", "ms_per_call": ms, "edges": ref_edges,
+        "same_edge_count": ref_edges == edges,
+        "calls": ref_calls, "note": "reference O(N^2) kernel <<<ceil(N/256),256>>>, kernel time only (CUDA events)"}
+    return out
 
 
 def reference_gpu_kernel(w, params, pos, types, table, radio, stream):

@@ -138,6 +138,8 @@ void free_particles(cf_world* w)
     dev_free(s.prox_count);
     dev_free(s.mesh_slots);
     dev_free(s.mesh_count);
+    dev_free(s.out_idx);
+    dev_free(s.colors);
     dev_free(s.counters);
     dev_free(s.cell_pop);
     dev_free(s.row_count);
@@ -251,12 +253,43 @@ int ensure_mesh(cf_world* w)
     return CF_OK;
 }
 
+// Staging for index output copied to host memory: grows to the largest
+// request and is kept, so repeated frames allocate nothing.
+int ensure_out(cf_world* w, size_t entries)
+{
+    Scratch& s = w->s;
+    if (entries <= s.out_cap) return CF_OK;
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    dev_free(s.out_idx);
+    s.out_idx = nullptr;
+    s.out_cap = 0;
+    CF_CUDA(dev_alloc(&s.out_idx, entries));
+    s.out_cap = entries;
+    return CF_OK;
+}
+
+// The colours of a vertex call, one per type, into the world's fixed colour
+// array (ordered on the stream before the kernel that reads them).
+int upload_colors(cf_world* w, const cf_color* colors)
+{
+    Scratch& s = w->s;
+    if (!s.colors) CF_CUDA(dev_alloc(&s.colors, 3 * (size_t)CF_MAX_TYPES));
+    float tmp[3 * CF_MAX_TYPES];
+    for (int t = 0; t < w->num_types; t++) {
+        tmp[3 * t] = colors[t].r;
+        tmp[3 * t + 1] = colors[t].g;
+        tmp[3 * t + 2] = colors[t].b;
+    }
+    CF_CUDA(cudaMemcpyAsync(s.colors, tmp, sizeof(float) * 3 * w->num_types, cudaMemcpyHostToDevice, w->stream));
+    return CF_OK;
+}
+
 // Wait for the world's stream and turn the device error word into a status.
 int sync_and_check(cf_world* w)
 {
-    int word = 0;
-    CF_CUDA(cudaMemcpyAsync(&word, w->err, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    CF_CUDA(cudaMemcpyAsync(&w->host_words[0], w->err, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
     CF_CUDA(cudaStreamSynchronize(w->stream));
+    const int word = w->host_words[0];
     if (word) {
         CF_CUDA(cudaMemsetAsync(w->err, 0, sizeof(int), w->stream));
         CF_CUDA(cudaStreamSynchronize(w->stream));
@@ -356,7 +389,7 @@ float certain_bound_impl(float thr, float max_extent)
     if (!(b > 0.0)) return 0.0f;
     int ex = 0;
     std::frexp(2.0 * (double)max_extent, &ex);
-    const double delta = 2.0 * std::ldexp(1.0, ex - 24);
+    const double delta = 3.0 * std::ldexp(1.0, ex - 24);
     const double lo = b - 3.47 * delta * std::sqrt(b) - 3.0 * delta * delta - 0x1p-20 * b;
     if (!(lo > 0.0)) return 0.0f;
     return nextafterf((float)lo, 0.0f);
@@ -364,8 +397,11 @@ float certain_bound_impl(float thr, float max_extent)
 
 // Bound for the force kernel's approximate pre-test: every pair whose exact
 // test fl(d^2 + 1e-4) < t passes fl(fma-contracted d^2 of a pre-shifted
-// displacement) < bound.  The displacements differ by at most delta per axis
-// (two roundings at the box scale); the rest is relative rounding slack.
+// displacement) < bound.  The kernel's displacement (candidate plus rounded
+// shift-minus-origin, less the rounded origin-relative home) and the
+// reference's (difference, then wrap) each differ from the exact shifted
+// difference by a few roundings at the box scale: together at most delta =
+// 3 ulp(2 * extent) per axis.  The rest is relative rounding slack.
 float filter_bound(float thr_max, float max_extent)
 {
     if (std::isinf(thr_max)) return INFINITY;
@@ -373,11 +409,12 @@ float filter_bound(float thr_max, float max_extent)
     if (!(b > 0.0)) return -1.0f;
     int ex = 0;
     std::frexp(2.0 * (double)max_extent, &ex);
-    const double delta = 2.0 * std::ldexp(1.0, ex - 24);  // 2 ulp of 2 * extent
+    const double delta = 3.0 * std::ldexp(1.0, ex - 24);  // 3 ulp of 2 * extent
     const double bound = (b + 3.47 * delta * std::sqrt(b) + 3.0 * delta * delta) * (1.0 + 0x1p-21);
-    // The kernel evaluates fma(dz, dz, fma(dy, dy, fma(dx, dx, -bound'))) < 0 and
-    // takes its sign bit: three roundings of magnitude <= 2^-24 max(d^2, bound')
-    // each, so bound' = bound (1 + 2^-19) keeps every pair below bound negative.
+    // On generic grids the kernel compares fma(dz, dz, fma(dy, dy, dx * dx)) with
+    // this: three roundings of at most 2^-24 max(d^2, bound') each, covered by
+    // bound' = bound (1 + 2^-19).  Elsewhere the kernel widens it again by the
+    // rounding of its expanded form (at the scale of the stencil box).
     return nextafterf((float)(bound * (1.0 + 0x1p-19)), INFINITY);
 }
 
@@ -691,6 +728,9 @@ int cf_create(int n, int num_types, float w_, float h_, float d_, uint64_t seed,
     w->stream = w->own_stream;
     e = dev_alloc(&w->err, 1);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc(error word)"));
+    e = cudaMallocHost(&w->host_words, 4 * sizeof(int));
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocHost(status words)"));
+    std::memset(w->host_words, 0, 4 * sizeof(int));
     e = cudaMemsetAsync(w->err, 0, sizeof(int), w->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemsetAsync"));
     e = dev_alloc(&w->tables, 1);
@@ -719,6 +759,7 @@ int cf_destroy(cf_world* w)
     drop_graphs(w);
     free_particles(w);
     dev_free(w->err);
+    if (w->host_words) cudaFreeHost(w->host_words);
     dev_free(w->tables);
     dev_free(w->world_tables);
     if (w->own_stream) cudaStreamDestroy(w->own_stream);
@@ -1233,8 +1274,9 @@ int cf_work_counters(cf_world* w, const cf_step_params* p, uint64_t* c27, uint64
 namespace {
 
 // Proximity selection: cell list with the proximity grid, per-particle
-// edges, exclusive scan.  Leaves offsets in prox_count[0..n].
-int proximity_prepare(cf_world* w, float distance, int max_conn, uint32_t* total)
+// edges, exclusive scan.  Enqueues only: offsets land in prox_count[0..n] and
+// the edge total in host_words[1] once the stream has reached this point.
+int proximity_enqueue(cf_world* w, float distance, int max_conn)
 {
     if (!(distance >= 0.0f) || !std::isfinite(distance)) return fail(CF_ERR_INVALID, "distance must be finite, >= 0");
     if (max_conn < 0 || max_conn > CF_MAX_PROX_CONN)
@@ -1251,14 +1293,16 @@ int proximity_prepare(cf_world* w, float distance, int max_conn, uint32_t* total
     CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_start, s.cell_end, g, w->n,
                                     dsq, max_conn, s.prox_slots, s.prox_count, w->stream));
     CF_CUDA(launch_scan_exclusive(s.prox_count, s.prox_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
-    CF_CUDA(cudaMemcpyAsync(total, s.prox_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
-    return sync_and_check(w);
+    CF_CUDA(cudaMemcpyAsync(&w->host_words[1], s.prox_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            w->stream));
+    return CF_OK;
 }
 
 // Triangle selection: cell list on the proximity grid of the mesh distance,
-// per-particle triangle counts, exclusive scan.  Leaves offsets in
-// mesh_count[0..n] and the triangle total in *total.
-int mesh_prepare(cf_world* w, float distance, int max_conn, uint32_t* total)
+// per-particle triangle counts, exclusive scan.  Enqueues only: offsets land
+// in mesh_count[0..n] and the triangle total in host_words[1] once the stream
+// has reached this point.
+int mesh_enqueue(cf_world* w, float distance, int max_conn)
 {
     if (!(distance >= 0.0f) || !std::isfinite(distance)) return fail(CF_ERR_INVALID, "distance must be finite, >= 0");
     if (max_conn < 0) return fail(CF_ERR_INVALID, "max_conn must be >= 0");
@@ -1277,38 +1321,49 @@ int mesh_prepare(cf_world* w, float distance, int max_conn, uint32_t* total)
     CF_CUDA(launch_mesh_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_start, s.cell_end, g, w->n, dsq,
                                std::min(max_conn, CF_MESH_MAX_CONN), s.mesh_slots, s.mesh_count, w->stream));
     CF_CUDA(launch_scan_exclusive(s.mesh_count, s.mesh_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
-    CF_CUDA(cudaMemcpyAsync(total, s.mesh_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    CF_CUDA(cudaMemcpyAsync(&w->host_words[1], s.mesh_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            w->stream));
+    return CF_OK;
+}
+
+// Copy `entries` int32 of the staging buffer to host memory and wait.
+int copy_out(cf_world* w, int32_t* host, size_t entries)
+{
+    CF_CUDA(cudaMemcpyAsync(host, w->s.out_idx, sizeof(int32_t) * entries, cudaMemcpyDeviceToHost, w->stream));
     return sync_and_check(w);
 }
 
 }  // namespace
 
+// Host output needs the total before the copy: one synchronisation for the
+// count, then the emit kernel into the kept staging buffer and the copy.
 int cf_triangle_mesh(cf_world* w, float distance, int max_conn, int32_t* triangles, int cap, int* n_triangles)
 {
     int rc = check_world(w);
     if (rc) return rc;
     if (cap < 0 || (cap > 0 && !triangles)) return fail(CF_ERR_INVALID, "bad triangle buffer");
-    uint32_t total = 0;
-    rc = mesh_prepare(w, distance, max_conn, &total);
+    rc = mesh_enqueue(w, distance, max_conn);
     if (rc) return rc;
+    rc = sync_and_check(w);
+    if (rc) return rc;
+    const uint32_t total = (uint32_t)w->host_words[1];
     if (n_triangles) *n_triangles = (int)total;
     const int write = (int)std::min<uint32_t>(total, (uint32_t)cap);
     if (write > 0) {
-        int32_t* d_tris = nullptr;
-        CF_CUDA(dev_alloc(&d_tris, 3 * (size_t)write));
-        cudaError_t e = launch_mesh_emit(w->s.mesh_slots, w->s.mesh_count, w->n, w->pos, nullptr, 1, d_tris, nullptr,
-                                         write, w->stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(triangles, d_tris, 12 * (size_t)write, cudaMemcpyDeviceToHost, w->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
-        cudaFree(d_tris);
-        if (e != cudaSuccess) return cuda_fail(e, "triangle mesh");
+        rc = ensure_out(w, 3 * (size_t)write);
+        if (rc) return rc;
+        CF_CUDA(launch_mesh_emit(w->s.mesh_slots, w->s.mesh_count, w->n, w->pos, nullptr, 1, w->s.out_idx, nullptr,
+                                 write, w->stream));
+        rc = copy_out(w, triangles, 3 * (size_t)write);
+        if (rc) return rc;
     }
     if (!triangles && cap == 0) return CF_OK;  // a count query
     if (total > (uint32_t)cap) return fail(CF_ERR_CAPACITY, "triangle buffer smaller than the triangle count");
     return CF_OK;
 }
 
+// Device output: the emit kernel stops at the caller's capacity by itself, so
+// selection, emission and the count read-back share one synchronisation.
 int cf_triangle_mesh_device(cf_world* w, float distance, int max_conn, const cf_color* colors, int n_colors,
                             float* vertices, int cap_vertices, int* vertex_count)
 {
@@ -1316,24 +1371,19 @@ int cf_triangle_mesh_device(cf_world* w, float distance, int max_conn, const cf_
     if (rc) return rc;
     if (!colors || n_colors < w->num_types) return fail(CF_ERR_INVALID, "need one colour per type");
     if (cap_vertices < 0 || (cap_vertices > 0 && !vertices)) return fail(CF_ERR_INVALID, "bad vertex buffer");
-    uint32_t total = 0;
-    rc = mesh_prepare(w, distance, max_conn, &total);
+    rc = mesh_enqueue(w, distance, max_conn);
     if (rc) return rc;
-    if (vertex_count) *vertex_count = (int)(3 * total);
-    const long long write = std::min<long long>(total, cap_vertices / 3);
-    if (write > 0) {
-        float* d_colors = nullptr;
-        CF_CUDA(dev_alloc(&d_colors, 3 * (size_t)w->num_types));
+    if (cap_vertices >= 3) {
         // ParticleSimulation.cu:356 indexes colours by type % numParticleTypes
-        cudaError_t e = cudaMemcpyAsync(d_colors, colors, sizeof(float) * 3 * w->num_types, cudaMemcpyHostToDevice,
-                                        w->stream);
-        if (e == cudaSuccess)
-            e = launch_mesh_emit(w->s.mesh_slots, w->s.mesh_count, w->n, w->pos, d_colors, w->num_types, nullptr,
-                                 vertices, write, w->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
-        cudaFree(d_colors);
-        if (e != cudaSuccess) return cuda_fail(e, "triangle mesh vertices");
+        rc = upload_colors(w, colors);
+        if (rc) return rc;
+        CF_CUDA(launch_mesh_emit(w->s.mesh_slots, w->s.mesh_count, w->n, w->pos, w->s.colors, w->num_types, nullptr,
+                                 vertices, cap_vertices / 3, w->stream));
     }
+    rc = sync_and_check(w);
+    if (rc) return rc;
+    const uint32_t total = (uint32_t)w->host_words[1];
+    if (vertex_count) *vertex_count = (int)(3 * total);
     if (!vertices && cap_vertices == 0) return CF_OK;  // a count query
     if (3 * (size_t)total > (size_t)cap_vertices) return fail(CF_ERR_CAPACITY, "vertex buffer too small");
     return CF_OK;
@@ -1344,21 +1394,20 @@ int cf_proximity_edges(cf_world* w, float distance, int max_conn, int32_t* edges
     int rc = check_world(w);
     if (rc) return rc;
     if (cap < 0 || (cap > 0 && !edges)) return fail(CF_ERR_INVALID, "bad edge buffer");
-    uint32_t total = 0;
-    rc = proximity_prepare(w, distance, max_conn, &total);
+    rc = proximity_enqueue(w, distance, max_conn);
     if (rc) return rc;
+    rc = sync_and_check(w);
+    if (rc) return rc;
+    const uint32_t total = (uint32_t)w->host_words[1];
     if (n_edges) *n_edges = (int)total;
     const int write = (int)std::min<uint32_t>(total, (uint32_t)cap);
     if (write > 0) {
-        int32_t* d_edges = nullptr;
-        CF_CUDA(dev_alloc(&d_edges, 2 * (size_t)write));
-        cudaError_t e = launch_proximity_emit_edges(w->s.prox_slots, w->s.prox_count, w->n, max_conn, d_edges, write,
-                                                    w->stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(edges, d_edges, 8 * (size_t)write, cudaMemcpyDeviceToHost, w->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
-        cudaFree(d_edges);
-        if (e != cudaSuccess) return cuda_fail(e, "proximity edges");
+        rc = ensure_out(w, 2 * (size_t)write);
+        if (rc) return rc;
+        CF_CUDA(launch_proximity_emit_edges(w->s.prox_slots, w->s.prox_count, w->n, max_conn, w->s.out_idx, write,
+                                            w->stream));
+        rc = copy_out(w, edges, 2 * (size_t)write);
+        if (rc) return rc;
     }
     if (total > (uint32_t)cap) return fail(CF_ERR_CAPACITY, "edge buffer smaller than the edge count");
     return CF_OK;
@@ -1371,23 +1420,19 @@ int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, cons
     if (rc) return rc;
     if (!colors || n_colors < w->num_types) return fail(CF_ERR_INVALID, "need one colour per type");
     if (cap_vertices < 0 || (cap_vertices > 0 && !vertices)) return fail(CF_ERR_INVALID, "bad vertex buffer");
-    uint32_t total = 0;
-    rc = proximity_prepare(w, distance, max_conn, &total);
+    rc = proximity_enqueue(w, distance, max_conn);
     if (rc) return rc;
-    if (vertex_count) *vertex_count = (int)(2 * total);
-    if (total > 0 && cap_vertices > 0) {
-        float* d_colors = nullptr;
-        CF_CUDA(dev_alloc(&d_colors, 3 * (size_t)w->num_types));
+    if (cap_vertices > 0) {
         // ParticleSimulation.cu:253 indexes colours by type % numParticleTypes
-        cudaError_t e = cudaMemcpyAsync(d_colors, colors, sizeof(float) * 3 * w->num_types, cudaMemcpyHostToDevice,
-                                        w->stream);
-        if (e == cudaSuccess)
-            e = launch_proximity_emit_vertices(w->s.prox_slots, w->s.prox_count, w->n, max_conn, w->pos, d_colors,
-                                               w->num_types, vertices, cap_vertices, w->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
-        cudaFree(d_colors);
-        if (e != cudaSuccess) return cuda_fail(e, "proximity vertices");
+        rc = upload_colors(w, colors);
+        if (rc) return rc;
+        CF_CUDA(launch_proximity_emit_vertices(w->s.prox_slots, w->s.prox_count, w->n, max_conn, w->pos, w->s.colors,
+                                               w->num_types, vertices, cap_vertices, w->stream));
     }
+    rc = sync_and_check(w);
+    if (rc) return rc;
+    const uint32_t total = (uint32_t)w->host_words[1];
+    if (vertex_count) *vertex_count = (int)(2 * total);
     if (2 * (size_t)total > (size_t)cap_vertices) return fail(CF_ERR_CAPACITY, "vertex buffer too small");
     return CF_OK;
 }

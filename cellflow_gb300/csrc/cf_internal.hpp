@@ -95,6 +95,10 @@ struct Scratch {
     uint32_t* mesh_count = nullptr; // n + 1 triangles per particle, exclusive-scanned in place
     uint32_t* scan_tmp = nullptr;   // block partials of the device-wide scan
     size_t scan_tmp_cap = 0;
+    // device staging of index output bound for host memory (edges, triangles)
+    int32_t* out_idx = nullptr;
+    size_t out_cap = 0;  // int32 entries
+    float* colors = nullptr;  // CF_MAX_TYPES * 3 floats: the colours of the last vertex call
     // work counters
     unsigned long long* counters = nullptr;  // [0] C27, [1] I
     uint32_t* cell_pop = nullptr;            // canonical-grid populations
@@ -176,6 +180,7 @@ struct cf_world {
     int* counts = nullptr;
     cf_particle* aos = nullptr;  // staging for AoS transfers (allocated on first use)
     int* err = nullptr;          // device error word
+    int* host_words = nullptr;   // pinned host: [0] error word read back, [1] output count read back
     cf::PairTables* tables = nullptr;
     cf::Scratch s;
     // host-side parameter surface

@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256)
     const uint32_t o = offsets[i], e_count = offsets[i + 1] - o;
     if (e_count == 0) return;
     const float4 a = pos[i];
-    const uint32_t c = __float_as_uint(a.w) % (uint32_t)n_colors;
+    const uint32_t c = (__float_as_uint(a.w) & kTypeMask) % (uint32_t)n_colors;
     const float r = colors[3 * c], gg = colors[3 * c + 1], b = colors[3 * c + 2];
     for (uint32_t e = 0; e < e_count; e++) {
         const uint32_t k = o + e;

@@ -10,14 +10,22 @@
 // the autotuner), with their periodic shift already applied, and every lane
 // tests every staged candidate (broadcast reads).
 //
+// Coordinates are staged relative to an origin per pass (the centre of the
+// stencil box where that keeps c - o exact, else 0), periodic shift folded
+// in, with |c|^2 beside them; an unshifted displacement is then the
+// reference's fl(c - h) bit for bit.
+//
 // Per batch of staged candidates, two phases per lane:
-//   Filter: squared distances of two candidates per instruction (packed f32x2
-//     add/mul/fma of sm_100+) against a bound that is >= the exact test for
-//     every pair; one 32-bit mask per 32 candidates.  ~85% of pairs stop here.
-//   Drain: for every set bit, the same contracted distance again; pairs whose
-//     distance is below a second bound (<= the exact test for every pair)
-//     interact for certain, and only the rare pairs between the two bounds
-//     (a band ~1e-6 wide) take the reference's exact test on the unshifted
+//   Filter: |c - h|^2 - bound = |c|^2 + (|h|^2 - bound) - 2 h.c for two
+//     candidates per instruction chain (packed f32x2 add/fma of sm_100+: one
+//     add and three fma per pair of candidates), the sign bit of each result
+//     shifted into a 32-bit mask per 32 candidates.  The bound is >= the
+//     exact test for every pair plus the expansion's rounding, which the
+//     origin keeps at the scale of the stencil box.  ~85% of pairs stop here.
+//   Drain: for every set bit, the contracted distance of the displacement;
+//     pairs below a second bound (<= the exact test for every pair) interact
+//     for certain, and only the rare pairs between the two bounds (a band
+//     ~1e-6 wide) take the reference's exact test on the unshifted
 //     coordinates.  Interacting pairs add their force term.
 //
 // Exactness (cuda-native/src/ParticleSimulation.cu:86-165):
@@ -71,13 +79,33 @@ __device__ __forceinline__ float staged_shift(float staged, float raw, float ext
 
 __device__ __forceinline__ int wrap_index(int v, int m) { return v < 0 ? v + m : (v >= m ? v - m : v); }
 
+// Staging origin on one axis for stencil cells [clo, chi] (shifted cell
+// coordinates, cell size cs) and the radius r of the box around it.  The
+// centre is used only where it is at least twice the half-width: then every
+// raw coordinate c in the box satisfies o/2 <= c <= 2o, so c - o is exact
+// (Sterbenz) and an unshifted displacement (c - o) - (h - o) rounds to the
+// reference's fl(c - h).  Otherwise the origin is 0 (also exact).
+__device__ __forceinline__ void stencil_origin(int clo, int chi, float cs, float& o, float& r)
+{
+    const float lo = (float)clo * cs, hi = (float)(chi + 1) * cs, mg = 0.05f * cs;
+    const float ctr = 0.5f * (lo + hi), half = 0.5f * (hi - lo) + mg;
+    if (ctr >= 2.0f * half) {
+        o = ctr;
+        r = half;
+    } else {
+        o = 0.0f;
+        r = fmaxf(fabsf(lo), fabsf(hi)) + mg;
+    }
+}
+
 // Per-warp staging area, kStage candidates (a multiple of 32) per batch.
 template <int kStage>
 struct WarpSmem {
     float4 xy[kStage / 2];              // staged (x_a, x_b, y_a, y_b) of slots 2p, 2p+1
-    float2 zz[kStage / 2];              // staged (z_a, z_b)
+    float4 zc[kStage / 2];              // staged (z_a, z_b, |c_a|^2, |c_b|^2)
     uint32_t meta[kStage];              // sorted index | type << 27
     uint32_t mask[(kStage / 32) * 32];  // [group][lane]
+    float origin[4];                    // the pass's staging origin (x, y, z)
 };
 
 struct Lane {
@@ -87,10 +115,18 @@ struct Lane {
     int count;
 };
 
+// The origin-relative home of a pass as the filter's packed operands:
+// (-2 h', -2 h') per axis and (|h'|^2 - bound) twice.  h' itself is
+// -0.5 * m2h exactly, so the drain's displacement fl(c' - h') is
+// fmaf(0.5, m2h, c').
+struct HomeOps {
+    float2 m2x, m2y, m2z, k;
+};
+
 // Per type pair of the item's world, T-stride: (R F, A F / eff).  With
-// s = d^2 + 1e-4 and rs = 1/sqrt(s), the reference's term
+// s = d^2 + 1e-4, dist = sqrt(s) and rs = 1/dist, the reference's term
 //   (d / dist) F (R exp(-k r^2) - A r),  r = dist / eff   (ParticleSimulation.cu:113-124)
-// is  d * rs * (R F * exp2(c1 s) - (A F / eff) * s rs),  c1 = -k log2(e) / eff^2.
+// is  d * (R F * exp2(c1 s) * rs - A F / eff),  c1 = -k log2(e) / eff^2.
 struct Tables {
     const float2* coef;  // (R F, A F / eff), T-stride
     const float* c1;     // 32-stride (unused with a uniform radius)
@@ -101,30 +137,34 @@ struct Tables {
 
 constexpr float kLog2e = 1.4426950408889634f;
 
-// Displacement from the home to a staged candidate: the filter's arithmetic.
+// Displacement from the home to a staged candidate.  Generic grids stage raw
+// coordinates and wrap per candidate; otherwise both ends are origin-relative
+// and the shift is already in the staged value.
 template <bool kGeneric>
 __device__ __forceinline__ void staged_delta(const StepConsts& c, float cx, float cy, float cz, const float4& h,
-                                             float& dx, float& dy, float& dz)
+                                             const HomeOps& H, float& dx, float& dy, float& dz)
 {
     if (kGeneric) {
         dx = wrap_ref(cx - h.x, c.ext[0], c.half[0]);
         dy = wrap_ref(cy - h.y, c.ext[1], c.half[1]);
         dz = wrap_ref(cz - h.z, c.ext[2], c.half[2]);
     } else {
-        dx = cx - h.x;
-        dy = cy - h.y;
-        dz = cz - h.z;
+        dx = fmaf(0.5f, H.m2x.x, cx);
+        dy = fmaf(0.5f, H.m2y.x, cy);
+        dz = fmaf(0.5f, H.m2z.x, cz);
     }
 }
 
 // One queued pair's interaction test: certain-interaction bound, exact
 // fallback.  Returns the staged displacement and its contracted d^2.
+// `origin` is the pass's staging origin (unused on generic grids).
 template <bool kGeneric, bool kUniformR>
-__device__ __forceinline__ bool pair_test(const StepConsts& c, const Lane& L, float cx, float cy, float cz,
-                                          uint32_t meta, const float4* __restrict__ pos_sorted, const Tables& tb,
-                                          float& dx, float& dy, float& dz, float& d2)
+__device__ __forceinline__ bool pair_test(const StepConsts& c, const Lane& L, const HomeOps& H,
+                                          const float* origin, float cx, float cy, float cz, uint32_t meta,
+                                          const float4* __restrict__ pos_sorted, const Tables& tb, float& dx,
+                                          float& dy, float& dz, float& d2)
 {
-    staged_delta<kGeneric>(c, cx, cy, cz, L.h, dx, dy, dz);
+    staged_delta<kGeneric>(c, cx, cy, cz, L.h, H, dx, dy, dz);
     d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     const uint32_t other = meta >> kTypeShift;
     const uint32_t pair = L.tp * kTableStride + other;
@@ -138,9 +178,9 @@ __device__ __forceinline__ bool pair_test(const StepConsts& c, const Lane& L, fl
             ey = wrap_ref(ey, c.ext[1], c.half[1]);
             ez = wrap_ref(ez, c.ext[2], c.half[2]);
         } else {
-            ex = __fadd_rn(ex, staged_shift(cx, o.x, c.ext[0]));
-            ey = __fadd_rn(ey, staged_shift(cy, o.y, c.ext[1]));
-            ez = __fadd_rn(ez, staged_shift(cz, o.z, c.ext[2]));
+            ex = __fadd_rn(ex, staged_shift(cx + origin[0], o.x, c.ext[0]));
+            ey = __fadd_rn(ey, staged_shift(cy + origin[1], o.y, c.ext[1]));
+            ez = __fadd_rn(ez, staged_shift(cz + origin[2], o.z, c.ext[2]));
         }
         const float e2 = __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
         inter = __fadd_rn(e2, 0.0001f) < (kUniformR ? c.thr_uniform : tb.thr[pair]);
@@ -159,16 +199,16 @@ __device__ __forceinline__ float pair_weight(float d2, uint32_t meta, const Lane
     const float c1 = kUniformR ? c1u : tb.c1[L.tp * kTableStride + other];
     float e;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(c1 * s));
-    return rs * fmaf(k.x, e, -k.y * (s * rs));
+    return fmaf(k.x * e, rs, -k.y);
 }
 
 // The staged coordinates of a slot.
-__device__ __forceinline__ void staged_xyz(const float* xyf, const float* zzf, int slot, float& x, float& y, float& z)
+__device__ __forceinline__ void staged_xyz(const float* xyf, const float* zcf, int slot, float& x, float& y, float& z)
 {
     const int pb = (slot >> 1) * 4 + (slot & 1);
     x = xyf[pb];
     y = xyf[pb + 2];
-    z = zzf[slot];
+    z = zcf[pb];
 }
 
 template <int kStage, int kMinBlocks, bool kGeneric, bool kUniformR>
@@ -185,6 +225,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     __shared__ float s_thr_lo[kUniformR ? 1 : kTableSize];
     extern __shared__ __align__(16) unsigned char s_dyn[];
     const int T = c.num_types;
+    // force coefficients, compact T-stride: one copy per block for a single
+    // world, one per warp (filled once its item's world is known) for a batch
+    const bool one_world = c.grid.worlds == 1;
+    float2* coef_base = reinterpret_cast<float2*>(s_dyn + sizeof(WarpSmem<kStage>) * kWarps);
     if (!kUniformR) {
         for (int e = threadIdx.x; e < T * T; e += kThreads) {
             const int a = e / T, b = e - a * T;
@@ -196,6 +240,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             s_thr_lo[k] = tables->threshold_lo[k];
         }
     }
+    if (one_world) {
+        for (int e = threadIdx.x; e < T * T; e += kThreads) {
+            const int a = e / T, b = e - a * T;
+            const float F = c.world_force[a * kTableStride + b];
+            const float inv = kUniformR ? c.inv_eff_uniform : 1.0f / tables->eff[a * kTableStride + b];
+            coef_base[e] = make_float2(c.repulsion * F, c.attraction * F * inv);
+        }
+    }
     __syncthreads();
     const float c1u = c.neg_k * kLog2e * c.inv_eff_uniform * c.inv_eff_uniform;
 
@@ -203,9 +255,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const int item = blockIdx.x * kWarps + warp;
     if (item >= *n_items) return;
     WarpSmem<kStage>& w = reinterpret_cast<WarpSmem<kStage>*>(s_dyn)[warp];
-    float2* wcoef = reinterpret_cast<float2*>(s_dyn + sizeof(WarpSmem<kStage>) * kWarps) + warp * T * T;
+    float2* wcoef = coef_base + (one_world ? 0 : warp * T * T);
     const float* xyf = reinterpret_cast<const float*>(w.xy);
-    const float* zzf = reinterpret_cast<const float*>(w.zz);
+    const float* zcf = reinterpret_cast<const float*>(w.zc);
     const int2 it = items[item];
     const bool active = lane < it.y;
     const int t = it.x + (active ? lane : 0);
@@ -227,14 +279,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const int yc = (int)((local_first / (uint32_t)mx) % (uint32_t)my);
     const int zc = (int)(local_first / (uint32_t)(mx * my));
     const int hx = (int)((keys_sorted[t] - world_base) % (uint32_t)mx);
-    // the world's force coefficients, compact T-stride
-    for (int e = lane; e < T * T; e += 32) {
-        const int a = e / T, b = e - a * T;
-        const float F = c.world_force[(size_t)world * kTableSize + a * kTableStride + b];
-        const float inv = kUniformR ? c.inv_eff_uniform : s_inv_eff[a * kTableStride + b];
-        wcoef[e] = make_float2(c.repulsion * F, c.attraction * F * inv);
+    if (!one_world) {
+        for (int e = lane; e < T * T; e += 32) {
+            const int a = e / T, b = e - a * T;
+            const float F = c.world_force[(size_t)world * kTableSize + a * kTableStride + b];
+            const float inv = kUniformR ? c.inv_eff_uniform : s_inv_eff[a * kTableStride + b];
+            wcoef[e] = make_float2(c.repulsion * F, c.attraction * F * inv);
+        }
+        __syncwarp();
     }
-    __syncwarp();
     const Tables tb{wcoef, s_c1, s_thr, s_thr_lo, T};
     // x sub-ranges whose union (range plus one cell each side) fits in the box
     const int width = kGeneric ? mx : (mx - 2);
@@ -245,12 +298,45 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         const int px0 = kGeneric ? x0 : x0 + pass * width;
         const int px1 = kGeneric ? x1 : min(x1, px0 + width - 1);
         const bool mine = active && (kGeneric || (hx >= px0 && hx <= px1));
-        // an idle home sits at -kFar: 2e30 from every candidate and from the +kFar padding slots
+        // generic grids: an idle home sits at -kFar, 2e30 from every candidate and from the
+        // +kFar padding slots
         const float hxf = mine ? L.h.x : -kFar, hyf = mine ? L.h.y : -kFar, hzf = mine ? L.h.z : -kFar;
 
         // segments: lane 2*row + half describes one contiguous range of the snapshot
         const int xlo = mx > 1 ? px0 - 1 : 0;
         const int xhi = mx > 1 ? min(px1 + 1, xlo + mx - 1) : 0;  // inclusive, at most mx cells
+
+        // Staging origin per axis (stencil_origin) for the stencil box (cells xlo..xhi,
+        // yc-1..yc+1, zc-1..zc+1 in shifted coordinates).  Every staged candidate and the
+        // homes lie within (rx, ry, rz) of it, so |c'|, |h'| <= R.  The expanded filter value
+        // |c'|^2 + (|h'|^2 - B) - 2 h'.c' carries at most 2^-24 (21 R^2 + 5 B) of rounding
+        // (three roundings in each square, one in the constant, four in the chain); the
+        // bound B = (thr_f (1 + 2^-18) + 2^-19 R^2)(1 + 2^-18) exceeds thr_f by more, so
+        // every pair whose staged d^2 is within thr_f stays negative.
+        HomeOps H;
+        float ox = 0.0f, oy = 0.0f, oz = 0.0f;
+        if (!kGeneric) {
+            float rx, ry, rz;
+            stencil_origin(xlo, xhi, c.ext[0] / (float)mx, ox, rx);
+            stencil_origin(yc - 1, yc + 1, c.ext[1] / (float)my, oy, ry);
+            stencil_origin(zc - 1, zc + 1, c.ext[2] / (float)mz, oz, rz);
+            const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
+            const float bnd = (thr_f * (1.0f + 0x1p-18f) + r2 * 0x1p-19f) * (1.0f + 0x1p-18f);
+            const float hpx = mine ? L.h.x - ox : 0.0f, hpy = mine ? L.h.y - oy : 0.0f,
+                        hpz = mine ? L.h.z - oz : 0.0f;
+            const float kk = mine ? fmaf(hpz, hpz, fmaf(hpy, hpy, hpx * hpx)) - bnd : kFar;
+            H.m2x = make_float2(-2.0f * hpx, -2.0f * hpx);
+            H.m2y = make_float2(-2.0f * hpy, -2.0f * hpy);
+            H.m2z = make_float2(-2.0f * hpz, -2.0f * hpz);
+            H.k = make_float2(kk, kk);
+            if (lane == 0) {
+                w.origin[0] = ox;
+                w.origin[1] = oy;
+                w.origin[2] = oz;
+            }
+        } else {
+            H.m2x = H.m2y = H.m2z = H.k = make_float2(0.0f, 0.0f);
+        }
         int seg_beg = 0, seg_len = 0;
         uint32_t seg_code = 0;
         const int ny = my > 1 ? 3 : 1, nz = mz > 1 ? 3 : 1;
@@ -305,30 +391,38 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 }
                 const int lo = max(pre, base), hi = min(pre + len, base + lim);
                 if (hi <= lo) continue;
-                const float sx = code_shift(code & 3u, c.ext[0]);
-                const float sy = code_shift((code >> 2) & 3u, c.ext[1]);
-                const float sz = code_shift(code >> 4, c.ext[2]);
+                // periodic shift less the origin (both zero on generic grids)
+                const float sx = code_shift(code & 3u, c.ext[0]) - ox;
+                const float sy = code_shift((code >> 2) & 3u, c.ext[1]) - oy;
+                const float sz = code_shift(code >> 4, c.ext[2]) - oz;
                 for (int g = lo + lane; g < hi; g += 32) {
                     const int slot = g - base;
                     const int j = beg + (g - pre);
                     const float4 p = pos_sorted[j];
                     float* xy = reinterpret_cast<float*>(&w.xy[slot >> 1]);
-                    float* zv = reinterpret_cast<float*>(&w.zz[slot >> 1]);
-                    xy[slot & 1] = p.x + sx;
-                    xy[2 + (slot & 1)] = p.y + sy;
-                    zv[slot & 1] = p.z + sz;
+                    float* zc = reinterpret_cast<float*>(&w.zc[slot >> 1]);
+                    const float x = p.x + sx, y = p.y + sy, z = p.z + sz;
+                    xy[slot & 1] = x;
+                    xy[2 + (slot & 1)] = y;
+                    zc[slot & 1] = z;
+                    zc[2 + (slot & 1)] = fmaf(z, z, fmaf(y, y, x * x));
                     w.meta[slot] = (uint32_t)j | ((__float_as_uint(p.w) & (kTableStride - 1)) << kTypeShift);
                 }
             }
-            // padding up to a whole group: never passes the filter
+            // padding up to a whole group: never passes the filter (at +kFar on generic
+            // grids, |c|^2 = kFar otherwise)
             for (int slot = lim + lane; slot < ngroups * 32; slot += 32) {
                 float* xy = reinterpret_cast<float*>(&w.xy[slot >> 1]);
-                float* zv = reinterpret_cast<float*>(&w.zz[slot >> 1]);
-                xy[slot & 1] = kFar;
-                xy[2 + (slot & 1)] = kFar;
-                zv[slot & 1] = kFar;
+                float* zc = reinterpret_cast<float*>(&w.zc[slot >> 1]);
+                const float far = kGeneric ? kFar : 0.0f;
+                xy[slot & 1] = far;
+                xy[2 + (slot & 1)] = far;
+                zc[slot & 1] = far;
+                zc[2 + (slot & 1)] = kFar;
             }
             __syncwarp();
+            const int own_g = own >> 5;  // -1 when the home is not in this batch
+            const uint32_t own_keep = ~(1u << (own & 31));
 
             // ---- filter: one bit per candidate
             if (kGeneric) {
@@ -339,35 +433,31 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         const int slot = gi * 32 + q;
                         if (slot >= lim) break;
                         float dx, dy, dz;
-                        staged_delta<true>(c, xyf[(slot >> 1) * 4 + (slot & 1)],
-                                           xyf[(slot >> 1) * 4 + 2 + (slot & 1)], zzf[slot], hh, dx, dy, dz);
+                        const int pb = (slot >> 1) * 4 + (slot & 1);
+                        staged_delta<true>(c, xyf[pb], xyf[pb + 2], zcf[pb], hh, H, dx, dy, dz);
                         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                         if (d2 < thr_f) m |= 1u << q;
                     }
-                    w.mask[gi * 32 + lane] = m;
+                    w.mask[gi * 32 + lane] = gi == own_g ? (m & own_keep) : m;
                 }
             } else {
-                const float2 nhx = make_float2(-hxf, -hxf), nhy = make_float2(-hyf, -hyf),
-                             nhz = make_float2(-hzf, -hzf), nthr = make_float2(-thr_f, -thr_f);
                 for (int gi = 0; gi < ngroups; gi++) {
-                    // d^2 - bound with the bound folded into the first FMA; the sign bit of
-                    // each result is shifted into the mask (last pair first, so pair p lands on
-                    // bits 2p, 2p + 1)
+                    // |c'|^2 + (|h'|^2 - bound) - 2 h'.c', two candidates per chain; the sign
+                    // bit of each result is shifted into the mask (last pair first, so pair p
+                    // lands on bits 2p, 2p + 1)
                     uint32_t m = 0;
 #pragma unroll
                     for (int p = 15; p >= 0; p--) {
                         const float4 a = w.xy[gi * 16 + p];
-                        const float2 b = w.zz[gi * 16 + p];
-                        const float2 dx = __fadd2_rn(make_float2(a.x, a.y), nhx);
-                        const float2 dy = __fadd2_rn(make_float2(a.z, a.w), nhy);
-                        const float2 dz = __fadd2_rn(b, nhz);
-                        float2 q = __ffma2_rn(dx, dx, nthr);
-                        q = __ffma2_rn(dy, dy, q);
-                        q = __ffma2_rn(dz, dz, q);
+                        const float4 b = w.zc[gi * 16 + p];
+                        float2 q = __fadd2_rn(make_float2(b.z, b.w), H.k);
+                        q = __ffma2_rn(make_float2(a.x, a.y), H.m2x, q);
+                        q = __ffma2_rn(make_float2(a.z, a.w), H.m2y, q);
+                        q = __ffma2_rn(make_float2(b.x, b.y), H.m2z, q);
                         m = __funnelshift_l(__float_as_uint(q.y), m, 1);
                         m = __funnelshift_l(__float_as_uint(q.x), m, 1);
                     }
-                    w.mask[gi * 32 + lane] = m;
+                    w.mask[gi * 32 + lane] = gi == own_g ? (m & own_keep) : m;
                 }
             }
 
@@ -382,19 +472,19 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 const bool has = m != 0u;
                 if (!__any_sync(0xffffffffu, has)) break;
                 if (has) {
+                    // the home's own slot was cleared from its mask by the filter
                     const int slot = gi * 32 + (__ffs(m) - 1);
                     m &= m - 1u;
-                    if (slot != own) {
-                        float x, y, z, dx, dy, dz, d2;
-                        staged_xyz(xyf, zzf, slot, x, y, z);
-                        const uint32_t meta = w.meta[slot];
-                        if (pair_test<kGeneric, kUniformR>(c, L, x, y, z, meta, pos_sorted, tb, dx, dy, dz, d2)) {
-                            const float wgt = pair_weight<kUniformR>(d2, meta, L, tb, c1u);
-                            L.count++;
-                            L.fx = fmaf(dx, wgt, L.fx);
-                            L.fy = fmaf(dy, wgt, L.fy);
-                            L.fz = fmaf(dz, wgt, L.fz);
-                        }
+                    float x, y, z, dx, dy, dz, d2;
+                    staged_xyz(xyf, zcf, slot, x, y, z);
+                    const uint32_t meta = w.meta[slot];
+                    if (pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta, pos_sorted, tb, dx, dy, dz,
+                                                       d2)) {
+                        const float wgt = pair_weight<kUniformR>(d2, meta, L, tb, c1u);
+                        L.count++;
+                        L.fx = fmaf(dx, wgt, L.fx);
+                        L.fy = fmaf(dy, wgt, L.fy);
+                        L.fz = fmaf(dz, wgt, L.fz);
                     }
                 }
             }
@@ -486,7 +576,9 @@ cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const 
                            const int2* items, const int* n_items, int blocks, float4* pos, float4* vel, float4* acc,
                            int* counts, cudaStream_t st)
 {
-    const size_t smem = (sizeof(WarpSmem<S>) + sizeof(float2) * c.num_types * c.num_types) * kWarps;
+    // staging per warp; force coefficients per block (one world) or per warp (a batch)
+    const size_t smem = sizeof(WarpSmem<S>) * kWarps +
+                        sizeof(float2) * c.num_types * c.num_types * (c.grid.worlds == 1 ? 1 : kWarps);
 #define CF_FORCE_LAUNCH(G, U)                                                                                        \
     step_force_kernel<S, B, G, U><<<blocks, kThreads, smem, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted,   \
                                                                   cell_off, items, n_items, pos, vel, acc, counts)

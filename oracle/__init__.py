@@ -164,6 +164,8 @@ def ref_gpu_lib() -> C.CDLL:
         L.cfref_gpu_step.argtypes = [vp, vp, vp, vp, vp, C.c_int, f, f, f, f, f, f, f, f, f, f, C.c_int, f, f,
                                      C.c_int, vp]
         L.cfref_gpu_step.restype = C.c_int
+        L.cfref_gpu_proximity.argtypes = [vp, C.c_int, f, C.c_int, vp, C.c_int, vp, vp, vp]
+        L.cfref_gpu_proximity.restype = C.c_int
         _ref_gpu = L
     return _ref_gpu
 
