@@ -71,7 +71,8 @@ struct StepConsts {
     float inv_eff_uniform;
     float thr_lo_uniform;  // contracted d^2 below this interacts for certain (uniform radius)
     float thr_filter;  // squared-distance bound of the approximate pre-test (>= every exact pass)
-    int variant;       // force-kernel variant (staging batch, occupancy), see cf_set_force_variant
+    int variant;       // force-kernel staging variant (batch size, occupancy): cf_set_force_variant % 4
+    int split;         // warps per item (1, 2, 4): 1 << (cf_set_force_variant / 4)
     float repulsion, attraction, neg_k, balance, force_multiplier, delta_t, friction;
     int max_expected_neighbors;
     const float* world_force;  // per-world force tables, kTableSize floats each (32-stride)
@@ -120,6 +121,10 @@ struct Scratch {
 
 // Cells of one tile of the CSR build (whole rows; 16 KB of shared memory).
 constexpr int kTileCellsMax = 4096;
+
+// Force-kernel staging variants (batch size and occupancy); a variant index
+// of cf_set_force_variant is stage + kForceStages * log2(warps per item).
+constexpr int kForceStages = 4;
 
 // Differentiable rollout: checkpoints, one segment of replayed states, the
 // adjoint buffers and the record of the last forward (cf_rollout_*).

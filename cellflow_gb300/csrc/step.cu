@@ -22,11 +22,12 @@
 //     shifted into a 32-bit mask per 32 candidates.  The bound is >= the
 //     exact test for every pair plus the expansion's rounding, which the
 //     origin keeps at the scale of the stencil box.  ~85% of pairs stop here.
-//   Drain: for every set bit, the contracted distance of the displacement;
-//     pairs below a second bound (<= the exact test for every pair) interact
-//     for certain, and only the rare pairs between the two bounds (a band
-//     ~1e-6 wide) take the reference's exact test on the unshifted
-//     coordinates.  Interacting pairs add their force term.
+//   Drain: for every set bit (two per trip, a warp-uniform trip count from
+//     the filter's per-lane hit counts), the contracted distance of the
+//     displacement; pairs below a second bound (<= the exact test for every
+//     pair) interact for certain, and only the rare pairs between the two
+//     bounds (a band ~1e-6 wide) take the reference's exact test on the
+//     unshifted coordinates.  Interacting pairs add their force term.
 //
 // Exactness (cuda-native/src/ParticleSimulation.cu:86-165):
 //   - the neighbour test is the reference's: d^2 = (dx*dx + dy*dy) + dz*dz and
@@ -223,6 +224,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     __shared__ float s_c1[kUniformR ? 1 : kTableSize];
     __shared__ float s_thr[kUniformR ? 1 : kTableSize];
     __shared__ float s_thr_lo[kUniformR ? 1 : kTableSize];
+    __shared__ float4 s_part[kWarps][32];  // partial sums of the item's other warps (split > 1)
     extern __shared__ __align__(16) unsigned char s_dyn[];
     const int T = c.num_types;
     // force coefficients, compact T-stride: one copy per block for a single
@@ -251,9 +253,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     __syncthreads();
     const float c1u = c.neg_k * kLog2e * c.inv_eff_uniform * c.inv_eff_uniform;
 
+    // c.split warps (1, 2 or 4) share an item, each taking an equal share of its
+    // candidates; part 0 adds the others' partial sums and integrates
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int item = blockIdx.x * kWarps + warp;
-    if (item >= *n_items) return;
+    const int split = c.split;
+    const int part = warp & (split - 1);
+    const int item = blockIdx.x * (kWarps / split) + warp / split;
+    if (item >= *n_items) return;  // the item's other warps leave too: no barrier is pending
     WarpSmem<kStage>& w = reinterpret_cast<WarpSmem<kStage>*>(s_dyn)[warp];
     float2* wcoef = coef_base + (one_world ? 0 : warp * T * T);
     const float* xyf = reinterpret_cast<const float*>(w.xy);
@@ -375,8 +381,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         const int total = __shfl_sync(0xffffffffu, seg_pre, 31);
         seg_pre -= seg_len;
 
-        for (int base = 0; base < total; base += kStage) {
-            const int lim = min(kStage, total - base);
+        const int share_lo = (int)((long long)total * part / split);
+        const int share_hi = (int)((long long)total * (part + 1) / split);
+        for (int base = share_lo; base < share_hi; base += kStage) {
+            const int lim = min(kStage, share_hi - base);
             const int ngroups = (lim + 31) >> 5;
             int own = -1;  // this lane's own slot in the batch (self exclusion)
             // ---- stage [base, base + lim) of the concatenated segments
@@ -423,6 +431,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             __syncwarp();
             const int own_g = own >> 5;  // -1 when the home is not in this batch
             const uint32_t own_keep = ~(1u << (own & 31));
+            int hits = 0;      // set bits of this lane in the batch
+            uint32_t nz = 0u;  // bit g: group g has a set bit
 
             // ---- filter: one bit per candidate
             if (kGeneric) {
@@ -438,7 +448,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
                         if (d2 < thr_f) m |= 1u << q;
                     }
-                    w.mask[gi * 32 + lane] = gi == own_g ? (m & own_keep) : m;
+                    const uint32_t mm = gi == own_g ? (m & own_keep) : m;
+                    w.mask[gi * 32 + lane] = mm;
+                    hits += __popc(mm);
+                    nz |= (mm != 0u ? 1u : 0u) << gi;
                 }
             } else {
                 for (int gi = 0; gi < ngroups; gi++) {
@@ -457,38 +470,78 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         m = __funnelshift_l(__float_as_uint(q.y), m, 1);
                         m = __funnelshift_l(__float_as_uint(q.x), m, 1);
                     }
-                    w.mask[gi * 32 + lane] = gi == own_g ? (m & own_keep) : m;
+                    const uint32_t mm = gi == own_g ? (m & own_keep) : m;
+                    w.mask[gi * 32 + lane] = mm;
+                    hits += __popc(mm);
+                    nz |= (mm != 0u ? 1u : 0u) << gi;
                 }
             }
 
-            // ---- drain: every set bit of this lane, in slot order
-            int gi = 0;
-            uint32_t m = w.mask[lane];
-            while (true) {
-                while (m == 0u && gi < ngroups - 1) {
-                    gi++;
-                    m = w.mask[gi * 32 + lane];
-                }
-                const bool has = m != 0u;
-                if (!__any_sync(0xffffffffu, has)) break;
-                if (has) {
-                    // the home's own slot was cleared from its mask by the filter
-                    const int slot = gi * 32 + (__ffs(m) - 1);
+            // ---- drain: every set bit of this lane in slot order, two per trip.  The trip
+            // count is uniform over the warp (the largest hit count, halved), and a lane
+            // whose current group mask runs out moves to the next non-empty group (the
+            // lowest remaining bit of nz) with one load: no nested loop, no vote per trip.
+            const int trips = (__reduce_max_sync(0xffffffffu, hits) + 1) >> 1;
+            int gi = nz ? __ffs(nz) - 1 : 0;
+            uint32_t m = w.mask[gi * 32 + lane];
+            for (int it = 0; it < trips; it++) {
+                if (2 * it < hits) {
+                    if (m == 0u) {
+                        nz &= nz - 1u;
+                        gi = __ffs(nz) - 1;  // a later group holds a hit: 2 it < hits
+                        m = w.mask[gi * 32 + lane];
+                    }
+                    const int sa = gi * 32 + (__ffs(m) - 1);
                     m &= m - 1u;
-                    float x, y, z, dx, dy, dz, d2;
-                    staged_xyz(xyf, zcf, slot, x, y, z);
-                    const uint32_t meta = w.meta[slot];
-                    if (pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta, pos_sorted, tb, dx, dy, dz,
-                                                       d2)) {
-                        const float wgt = pair_weight<kUniformR>(d2, meta, L, tb, c1u);
+                    const bool hb = 2 * it + 1 < hits;
+                    if (hb && m == 0u) {
+                        nz &= nz - 1u;
+                        gi = __ffs(nz) - 1;
+                        m = w.mask[gi * 32 + lane];
+                    }
+                    const int sb = hb ? gi * 32 + (__ffs(m) - 1) : sa;
+                    if (hb) m &= m - 1u;
+                    // both pairs are evaluated side by side (the second repeats the first
+                    // when the lane has one hit left and is then not accumulated)
+                    float xa, ya, za, dxa, dya, dza, d2a, xb, yb, zb, dxb, dyb, dzb, d2b;
+                    staged_xyz(xyf, zcf, sa, xa, ya, za);
+                    staged_xyz(xyf, zcf, sb, xb, yb, zb);
+                    const uint32_t ma = w.meta[sa], mb = w.meta[sb];
+                    const bool ia = pair_test<kGeneric, kUniformR>(c, L, H, w.origin, xa, ya, za, ma, pos_sorted, tb,
+                                                                   dxa, dya, dza, d2a);
+                    const bool ib = hb && pair_test<kGeneric, kUniformR>(c, L, H, w.origin, xb, yb, zb, mb,
+                                                                         pos_sorted, tb, dxb, dyb, dzb, d2b);
+                    const float wa = pair_weight<kUniformR>(d2a, ma, L, tb, c1u);
+                    const float wb = pair_weight<kUniformR>(ib ? d2b : d2a, mb, L, tb, c1u);
+                    if (ia) {
                         L.count++;
-                        L.fx = fmaf(dx, wgt, L.fx);
-                        L.fy = fmaf(dy, wgt, L.fy);
-                        L.fz = fmaf(dz, wgt, L.fz);
+                        L.fx = fmaf(dxa, wa, L.fx);
+                        L.fy = fmaf(dya, wa, L.fy);
+                        L.fz = fmaf(dza, wa, L.fz);
+                    }
+                    if (ib) {
+                        L.count++;
+                        L.fx = fmaf(dxb, wb, L.fx);
+                        L.fy = fmaf(dyb, wb, L.fy);
+                        L.fz = fmaf(dzb, wb, L.fz);
                     }
                 }
             }
             __syncwarp();
+        }
+    }
+    if (split > 1) {
+        // the item's warps meet at a named barrier (id 1 + item slot, 32 * split threads);
+        // part 0 adds the partial sums in part order, so the result is deterministic
+        if (part != 0) s_part[warp][lane] = make_float4(L.fx, L.fy, L.fz, __int_as_float(L.count));
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + warp / split), "r"(32 * split) : "memory");
+        if (part != 0) return;
+        for (int q = 1; q < split; q++) {
+            const float4 v = s_part[warp + q][lane];
+            L.fx += v.x;
+            L.fy += v.y;
+            L.fz += v.z;
+            L.count += __float_as_int(v.w);
         }
     }
     if (!active) return;
@@ -628,7 +681,8 @@ cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, con
                               float4* acc, int* counts, cudaStream_t st)
 {
     if (c.n <= 0 || max_items <= 0) return cudaSuccess;
-    const int blocks = (max_items + kWarps - 1) / kWarps;
+    if (c.split != 1 && c.split != 2 && c.split != 4) return cudaErrorInvalidValue;
+    const int blocks = (int)(((long long)max_items * c.split + kWarps - 1) / kWarps);
     switch (c.variant) {
     case 1:
         return launch_variant<256, 6>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,

@@ -180,11 +180,15 @@ float cf_lfo_ratio(float ratio, float lfo_a, float lfo_s, float t_seconds);
  * builds the cell list, computes forces, neighbour counts and the
  * density-adaptive scale, integrates and wraps.  Asynchronous. */
 int cf_step(cf_world* w, const cf_step_params* p, int nsteps);
-/* Force-kernel variants: 0 = 256 candidates staged per warp batch, register
- * budget for 8 blocks per SM; 1 = 256 staged, 6 blocks per SM; 2 = 512
- * staged, 4 blocks per SM; 3 = 384 staged, 6 blocks per SM.  Results are
- * bit-identical across variants. */
-#define CF_FORCE_VARIANTS 4
+/* Force-kernel variants: v % 4 picks the staging: 0 = 256 candidates staged
+ * per warp batch, register budget for 8 blocks per SM; 1 = 256 staged, 6
+ * blocks per SM; 2 = 512 staged, 4 blocks per SM; 3 = 384 staged, 6 blocks
+ * per SM.  v / 4 picks the warps per 32-particle item: 1, 2 or 4 (each warp
+ * takes an equal share of the item's candidates; more warps for worlds too
+ * small to fill the GPU).  Results are bit-identical across stagings; with
+ * 2 or 4 warps the partial sums are added in a fixed order, which differs
+ * from the single-warp order by rounding only. */
+#define CF_FORCE_VARIANTS 12
 /* Autotuner of the step (no counterpart in the reference): runs `steps`
  * trial steps with each force-kernel variant, restores the particle state,
  * keeps the fastest variant for later steps and returns it in

@@ -160,27 +160,38 @@ def test_rollout_short(cflib):
 
 
 def test_autotune_keeps_state_and_results(cflib):
-    """All force-kernel variants give bit-identical steps; autotuning restores the state."""
+    """Force-kernel stagings give bit-identical steps; splitting an item over 2 or 4 warps
+    changes only the summation order (same counts, forces within rounding); autotuning
+    restores the state."""
     w = inputs.Workload("tune", n=30000, num_types=5, radius=0.12, steps=1, seed=19)
     params = w.params()
     sim, pos, types, table, radio = make_world(w)
     before = sim.get_state()
     chosen = sim.autotune(params, 2)
-    assert chosen in range(4)
+    assert chosen in range(12)
     after = sim.get_state()
     for a, b in zip(before, after):
         assert np.array_equal(a, b)
     sim.close()
-    results = []
-    for variant in range(4):
+    results, counts = {}, {}
+    for variant in range(12):
         s, *_ = make_world(w, pos, types, table, radio)
         s.set_force_variant(variant)
-        s.simulate(params, 2)
-        results.append(s.getParticleData())
+        s.simulate(params, 1)
+        results[variant] = s.getParticleData()
+        counts[variant] = s.getNeighborCounts()
         s.close()
-    for rec in results[1:]:
+    for variant in range(12):
+        same_split = variant - variant % 4
         for f in ("pos", "vel", "acc"):
-            assert np.array_equal(results[0][f], rec[f]), f
+            assert np.array_equal(results[same_split][f], results[variant][f]), (variant, f)
+        assert np.array_equal(counts[0], counts[variant]), variant
+        scale = np.abs(results[0]["acc"]).max()
+        assert np.abs(results[0]["acc"] - results[variant]["acc"]).max() <= 1e-6 * scale, variant
+    s, *_ = make_world(w, pos, types, table, radio)
+    with pytest.raises(CellFlowError):
+        s.set_force_variant(12)
+    s.close()
 
 
 def test_zero_table_is_pure_friction(cflib):
