@@ -17,10 +17,11 @@
 //   gM += adapt_i (f_i . ga_i),  gb += M density_i (f_i . ga_i),  gfriction += v . gw.
 //
 // Kernels: adj_prep (per particle: gv, gf and ga staged in cell order) and
-// adj_pair (one thread per home particle in cell order, 27-cell stencil,
-// the reference's exact neighbour test on the stored positions so the
-// neighbour sets are the forward's).  Table and parameter gradients collect
-// in shared memory per block and are added to double accumulators.
+// adj_pair (one warp per home particle in cell order, the lanes striding over
+// its 27-cell stencil, the reference's exact neighbour test on the stored
+// positions so the neighbour sets are the forward's).  Table and parameter
+// gradients collect in shared memory per block and are added to double
+// accumulators.
 //
 // Soft radial distribution: bins of width D = r_max / bins, centres
 // c_k = (k + 1/2) D, cubic B-spline weights B((r - c_k) / D) (support 2 bins
@@ -28,12 +29,30 @@
 //   h[a][b][k] = sum_{i in a, j in b, j != i} B((r_ij - c_k) / D) / (N_a (N_b / V) 4 pi c_k^2 D).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "cf_internal.hpp"
 
 namespace cf {
 namespace {
 
 constexpr int kAdjThreads = 128;
+
+// Streaming multiprocessors of the current device (queried once; a query,
+// so also legal while a stream is being captured).
+int num_sms()
+{
+    static int sms = 0;
+    if (sms <= 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            sms = v;
+        else
+            return 148;
+    }
+    return sms;
+}
 
 __device__ __forceinline__ float wrap_ref(float d, float ext, float half)
 {
@@ -87,6 +106,35 @@ __global__ void adj_prep_kernel(StepConsts c, const uint32_t* __restrict__ vals,
     if ((threadIdx.x & 31) == 0 && part != 0.0f) atomicAdd(&gacc[kTableSize + CF_GRAD_FRICTION], (double)part);
 }
 
+// The x cells cx-1..cx+1 of a stencil row (fewer on axes under 3 cells) as
+// at most two runs of consecutive cells, [a0, b0] and [a1, b1] (b1 < a1: none).
+__device__ __forceinline__ void x_runs(int cx, int m0, int& a0, int& b0, int& a1, int& b1)
+{
+    int xlo, xhi;
+    axis_range(m0, xlo, xhi);
+    const int lo = cx + xlo, hi = cx + xhi;
+    a1 = 0;
+    b1 = -1;
+    if (lo < 0) {
+        a0 = lo + m0;
+        b0 = m0 - 1;
+        b1 = hi;
+    } else if (hi >= m0) {
+        a0 = lo;
+        b0 = m0 - 1;
+        b1 = hi - m0;
+    } else {
+        a0 = lo;
+        b0 = hi;
+    }
+}
+
+// One warp per home particle (grid-stride over homes in cell order): the
+// lanes share the home's 27-cell stencil, nine rows of at most two runs of
+// consecutive cells, i.e. contiguous ranges of the sorted snapshot, and
+// stride over them; the warp then sums its partials.  The neighbour test is
+// the reference's exact one on the stored positions, so the neighbour sets
+// are the forward's.
 __global__ void __launch_bounds__(kAdjThreads)
     adj_pair_kernel(StepConsts c, const PairTables* __restrict__ tables, const float4* __restrict__ pos_sorted,
                     const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
@@ -99,36 +147,41 @@ __global__ void __launch_bounds__(kAdjThreads)
     if (threadIdx.x < 8) s_par[threadIdx.x] = 0.0f;
     __syncthreads();
 
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int warps = (int)(gridDim.x * (blockDim.x >> 5));
+    const float R = c.repulsion, A = c.attraction, kk = -c.neg_k;
+    const int m0 = c.grid.m[0], m1 = c.grid.m[1], m2 = c.grid.m[2];
+    int ylo, yhi, zlo, zhi;
+    axis_range(m1, ylo, yhi);
+    axis_range(m2, zlo, zhi);
     float pR = 0.0f, pA = 0.0f, pK = 0.0f, pM = 0.0f, pB = 0.0f;
-    if (k < c.n) {
+    for (int k = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); k < c.n; k += warps) {
         const float4 h = pos_sorted[k];
         const uint32_t ti = type_of(h);
         const float4 gfi = gf_sorted[k];
-        const int m0 = c.grid.m[0], m1 = c.grid.m[1], m2 = c.grid.m[2];
         const uint32_t cell = keys[k];
         const int cx = (int)(cell % (uint32_t)m0), cy = (int)((cell / (uint32_t)m0) % (uint32_t)m1),
                   cz = (int)(cell / ((uint32_t)m0 * (uint32_t)m1));
-        int xlo, xhi, ylo, yhi, zlo, zhi;
-        axis_range(m0, xlo, xhi);
-        axis_range(m1, ylo, yhi);
-        axis_range(m2, zlo, zhi);
-        const float R = c.repulsion, A = c.attraction, kk = -c.neg_k;
+        int a0, b0, a1, b1;
+        x_runs(cx, m0, a0, b0, a1, b1);
         float ax = 0.0f, ay = 0.0f, az = 0.0f;  // pair part of gx_i
         float fx = 0.0f, fy = 0.0f, fz = 0.0f;  // unscaled force f_i
         for (int oz = zlo; oz <= zhi; oz++)
-            for (int oy = ylo; oy <= yhi; oy++)
-                for (int ox = xlo; ox <= xhi; ox++) {
-                    const int c2 = (wrap_cell(cz + oz, m2) * m1 + wrap_cell(cy + oy, m1)) * m0 + wrap_cell(cx + ox, m0);
-                    const uint32_t qb = cell_off[c2], qe = cell_off[c2 + 1];
-                    for (uint32_t q = qb; q < qe; q++) {
+            for (int oy = ylo; oy <= yhi; oy++) {
+                const int row = (wrap_cell(cz + oz, m2) * m1 + wrap_cell(cy + oy, m1)) * m0;
+                for (int run = 0; run < 2; run++) {
+                    const int ra = run ? a1 : a0, rb = run ? b1 : b0;
+                    if (rb < ra) continue;
+                    const uint32_t qb = cell_off[row + ra], qe = cell_off[row + rb + 1];
+                    for (uint32_t q = qb + lane; q < qe; q += 32) {
                         if ((int)q == k) continue;
                         const float4 o = pos_sorted[q];
                         // the reference's displacement and neighbour test (ParticleSimulation.cu:97-111)
                         const float dx = wrap_ref(__fsub_rn(o.x, h.x), c.ext[0], c.half[0]);
                         const float dy = wrap_ref(__fsub_rn(o.y, h.y), c.ext[1], c.half[1]);
                         const float dz = wrap_ref(__fsub_rn(o.z, h.z), c.ext[2], c.half[2]);
-                        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                        const float d2 =
+                            __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
                         const float s = __fadd_rn(d2, 0.0001f);
                         const uint32_t tj = type_of(o);
                         const int pair = ti * kTableStride + tj;
@@ -161,23 +214,30 @@ __global__ void __launch_bounds__(kAdjThreads)
                         fz += fw * dz;
                     }
                 }
-        const uint32_t i = vals[k];
-        float4 g = gx[i];
-        g.x += ax;
-        g.y += ay;
-        g.z += az;
-        gx[i] = g;
-        const float4 ga = ga_sorted[k];
-        const float fga = fx * ga.x + fy * ga.y + fz * ga.z;
-        pM = (1.0f - (1.0f - c.balance) * ga.w) * fga;
-        pB = c.force_multiplier * ga.w * fga;
+            }
+        ax = warp_sum(ax);
+        ay = warp_sum(ay);
+        az = warp_sum(az);
+        fx = warp_sum(fx);
+        fy = warp_sum(fy);
+        fz = warp_sum(fz);
+        if (lane == 0) {
+            const uint32_t i = vals[k];
+            float4 g = gx[i];
+            g.x += ax;
+            g.y += ay;
+            g.z += az;
+            gx[i] = g;
+            const float4 ga = ga_sorted[k];
+            const float fga = fx * ga.x + fy * ga.y + fz * ga.z;
+            pM += (1.0f - (1.0f - c.balance) * ga.w) * fga;
+            pB += c.force_multiplier * ga.w * fga;
+        }
     }
     pR = warp_sum(pR);
     pA = warp_sum(pA);
     pK = warp_sum(pK);
-    pM = warp_sum(pM);
-    pB = warp_sum(pB);
-    if ((threadIdx.x & 31) == 0) {
+    if (lane == 0) {
         atomicAdd(&s_par[CF_GRAD_REPULSION], pR);
         atomicAdd(&s_par[CF_GRAD_ATTRACTION], pA);
         atomicAdd(&s_par[CF_GRAD_K], pK);
@@ -407,8 +467,10 @@ cudaError_t launch_adjoint_step(const StepConsts& c, const PairTables* tables, c
     const int blocks = (c.n + kAdjThreads - 1) / kAdjThreads;
     adj_prep_kernel<<<blocks, kAdjThreads, 0, st>>>(c, vals_sorted, vel, cnt_prev, cnt_new, gx, gv, gf_sorted,
                                                      ga_sorted, gacc);
-    adj_pair_kernel<<<blocks, kAdjThreads, 0, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off,
-                                                     gf_sorted, ga_sorted, gx, gacc);
+    // one warp per home, grid-stride: four blocks of four warps per SM
+    const int pair_blocks = std::min((c.n + kAdjThreads / 32 - 1) / (kAdjThreads / 32), 4 * num_sms());
+    adj_pair_kernel<<<pair_blocks, kAdjThreads, 0, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off,
+                                                          gf_sorted, ga_sorted, gx, gacc);
     return cudaGetLastError();
 }
 

@@ -109,6 +109,18 @@ struct WarpSmem {
     float origin[4];                    // the pass's staging origin (x, y, z)
 };
 
+// Named barrier of the warps sharing an item: id 1 + slot (slot < kWarps),
+// immediate ids so only five hardware barriers are reserved.
+__device__ __forceinline__ void item_barrier(int slot, int threads)
+{
+    switch (slot) {
+    case 0: asm volatile("bar.sync 1, %0;" ::"r"(threads) : "memory"); break;
+    case 1: asm volatile("bar.sync 2, %0;" ::"r"(threads) : "memory"); break;
+    case 2: asm volatile("bar.sync 3, %0;" ::"r"(threads) : "memory"); break;
+    default: asm volatile("bar.sync 4, %0;" ::"r"(threads) : "memory"); break;
+    }
+}
+
 struct Lane {
     float4 h;     // home position (raw)
     uint32_t tp;  // home type
@@ -252,6 +264,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     }
     __syncthreads();
     const float c1u = c.neg_k * kLog2e * c.inv_eff_uniform * c.inv_eff_uniform;
+    // pairs per drain trip: two side by side where the register budget allows
+    constexpr int kPer = kMinBlocks >= 8 ? 1 : 2;
 
     // c.split warps (1, 2 or 4) share an item, each taking an equal share of its
     // candidates; part 0 adds the others' partial sums and integrates
@@ -477,53 +491,52 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 }
             }
 
-            // ---- drain: every set bit of this lane in slot order, two per trip.  The trip
-            // count is uniform over the warp (the largest hit count, halved), and a lane
+            // ---- drain: every set bit of this lane in slot order, kPer per trip.  The trip
+            // count is uniform over the warp (the largest hit count over kPer), and a lane
             // whose current group mask runs out moves to the next non-empty group (the
             // lowest remaining bit of nz) with one load: no nested loop, no vote per trip.
-            const int trips = (__reduce_max_sync(0xffffffffu, hits) + 1) >> 1;
+            // A lane with fewer than kPer hits left repeats its first pair of the trip
+            // without accumulating it.
+            const int trips = (__reduce_max_sync(0xffffffffu, hits) + kPer - 1) / kPer;
             int gi = nz ? __ffs(nz) - 1 : 0;
             uint32_t m = w.mask[gi * 32 + lane];
             for (int it = 0; it < trips; it++) {
-                if (2 * it < hits) {
-                    if (m == 0u) {
-                        nz &= nz - 1u;
-                        gi = __ffs(nz) - 1;  // a later group holds a hit: 2 it < hits
-                        m = w.mask[gi * 32 + lane];
+                if (kPer * it < hits) {
+                    int slot[kPer];
+                    bool valid[kPer];
+#pragma unroll
+                    for (int q = 0; q < kPer; q++) {
+                        valid[q] = kPer * it + q < hits;
+                        if (valid[q] && m == 0u) {
+                            nz &= nz - 1u;
+                            gi = __ffs(nz) - 1;  // a later group holds a hit
+                            m = w.mask[gi * 32 + lane];
+                        }
+                        slot[q] = valid[q] ? gi * 32 + (__ffs(m) - 1) : slot[0];
+                        if (valid[q]) m &= m - 1u;
                     }
-                    const int sa = gi * 32 + (__ffs(m) - 1);
-                    m &= m - 1u;
-                    const bool hb = 2 * it + 1 < hits;
-                    if (hb && m == 0u) {
-                        nz &= nz - 1u;
-                        gi = __ffs(nz) - 1;
-                        m = w.mask[gi * 32 + lane];
+                    float dx[kPer], dy[kPer], dz[kPer], d2[kPer], wgt[kPer];
+                    uint32_t meta[kPer];
+                    bool inter[kPer];
+#pragma unroll
+                    for (int q = 0; q < kPer; q++) {
+                        float x, y, z;
+                        staged_xyz(xyf, zcf, slot[q], x, y, z);
+                        meta[q] = w.meta[slot[q]];
+                        inter[q] = pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta[q], pos_sorted, tb,
+                                                                  dx[q], dy[q], dz[q], d2[q]) &&
+                                   valid[q];
                     }
-                    const int sb = hb ? gi * 32 + (__ffs(m) - 1) : sa;
-                    if (hb) m &= m - 1u;
-                    // both pairs are evaluated side by side (the second repeats the first
-                    // when the lane has one hit left and is then not accumulated)
-                    float xa, ya, za, dxa, dya, dza, d2a, xb, yb, zb, dxb, dyb, dzb, d2b;
-                    staged_xyz(xyf, zcf, sa, xa, ya, za);
-                    staged_xyz(xyf, zcf, sb, xb, yb, zb);
-                    const uint32_t ma = w.meta[sa], mb = w.meta[sb];
-                    const bool ia = pair_test<kGeneric, kUniformR>(c, L, H, w.origin, xa, ya, za, ma, pos_sorted, tb,
-                                                                   dxa, dya, dza, d2a);
-                    const bool ib = hb && pair_test<kGeneric, kUniformR>(c, L, H, w.origin, xb, yb, zb, mb,
-                                                                         pos_sorted, tb, dxb, dyb, dzb, d2b);
-                    const float wa = pair_weight<kUniformR>(d2a, ma, L, tb, c1u);
-                    const float wb = pair_weight<kUniformR>(ib ? d2b : d2a, mb, L, tb, c1u);
-                    if (ia) {
-                        L.count++;
-                        L.fx = fmaf(dxa, wa, L.fx);
-                        L.fy = fmaf(dya, wa, L.fy);
-                        L.fz = fmaf(dza, wa, L.fz);
-                    }
-                    if (ib) {
-                        L.count++;
-                        L.fx = fmaf(dxb, wb, L.fx);
-                        L.fy = fmaf(dyb, wb, L.fy);
-                        L.fz = fmaf(dzb, wb, L.fz);
+#pragma unroll
+                    for (int q = 0; q < kPer; q++) wgt[q] = pair_weight<kUniformR>(d2[q], meta[q], L, tb, c1u);
+#pragma unroll
+                    for (int q = 0; q < kPer; q++) {
+                        if (inter[q]) {
+                            L.count++;
+                            L.fx = fmaf(dx[q], wgt[q], L.fx);
+                            L.fy = fmaf(dy[q], wgt[q], L.fy);
+                            L.fz = fmaf(dz[q], wgt[q], L.fz);
+                        }
                     }
                 }
             }
@@ -534,7 +547,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         // the item's warps meet at a named barrier (id 1 + item slot, 32 * split threads);
         // part 0 adds the partial sums in part order, so the result is deterministic
         if (part != 0) s_part[warp][lane] = make_float4(L.fx, L.fy, L.fz, __int_as_float(L.count));
-        asm volatile("bar.sync %0, %1;" ::"r"(1 + warp / split), "r"(32 * split) : "memory");
+        item_barrier(warp / split, 32 * split);
         if (part != 0) return;
         for (int q = 1; q < split; q++) {
             const float4 v = s_part[warp + q][lane];
