@@ -269,6 +269,7 @@ constexpr int kTileWarps = kTileThreads / 32;
 
 struct TileGeom {
     int m0;             // cells per row
+    int m1, m2;         // cells along y and z (a row r is y = r % m1, z = r / m1 % m2, world = r / (m1 m2))
     int rows;           // rows of the whole grid (all worlds)
     int rows_per_tile;  // whole rows per tile: floor(kTileCellsMax / m0) >= 1
     int tiles;
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(kTileThreads)
 }
 
 __global__ void __launch_bounds__(kTileThreads)
-    tile_apply_kernel(uint32_t* cell_off, TileGeom tg, const uint2* __restrict__ tile_sums, int2* __restrict__ items,
+    tile_apply_kernel(uint32_t* cell_off, TileGeom tg, const uint2* __restrict__ tile_sums, Item* __restrict__ items,
                       int* __restrict__ n_items)
 {
     __shared__ uint32_t s_off[kTileCellsMax + 1];
@@ -399,7 +400,9 @@ __global__ void __launch_bounds__(kTileThreads)
         if (r >= L.nr) break;
         const uint32_t start = prefix_p + s_off[r * tg.m0];
         const uint32_t cnt = s_off[(r + 1) * tg.m0] - s_off[r * tg.m0];
-        for (uint32_t k = 0; k < cnt; k += 32u) items[item++] = make_int2((int)(start + k), (int)min(32u, cnt - k));
+        const int gr = L.r0 + r, yz_w = gr / tg.m1;
+        const int yz = (gr - yz_w * tg.m1) | ((yz_w % tg.m2) << 16), world = yz_w / tg.m2;
+        for (uint32_t k = 0; k < cnt; k += 32u) items[item++] = Item{(int)(start + k), (int)min(32u, cnt - k), yz, world};
     }
     if (last && threadIdx.x == 0) *n_items = (int)(prefix_i + L.items);
 }
@@ -615,7 +618,7 @@ int cell_list_tiles(const Grid& g)
 }
 
 cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
-                                 Scratch& s, uint32_t* cell_off, int2* items, int* n_items, int* err, int* which,
+                                 Scratch& s, uint32_t* cell_off, Item* items, int* n_items, int* err, int* which,
                                  cudaStream_t st)
 {
     cudaError_t e = cudaMemsetAsync(cell_off, 0, sizeof(uint32_t) * ((size_t)g.cells + 1), st);
@@ -635,6 +638,8 @@ cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const 
     }
     TileGeom tg;
     tg.m0 = g.m[0];
+    tg.m1 = g.m[1];
+    tg.m2 = g.m[2];
     tg.rows = g.cells / g.m[0];
     tg.rows_per_tile = kTileCellsMax / g.m[0];
     tg.tiles = tiles;

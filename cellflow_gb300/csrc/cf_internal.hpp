@@ -78,6 +78,15 @@ struct StepConsts {
     const float* world_force;  // per-world force tables, kTableSize floats each (32-stride)
 };
 
+// One force-kernel item: up to 32 consecutive sorted particles of one row of
+// cells, with the row's cell coordinates inside its world.
+struct __align__(16) Item {
+    int first;  // first sorted index
+    int count;  // particles, 1..32
+    int yz;     // y | z << 16
+    int world;
+};
+
 struct Scratch {
     uint32_t* keys[2] = {nullptr, nullptr};
     uint32_t* vals[2] = {nullptr, nullptr};
@@ -110,7 +119,7 @@ struct Scratch {
     // force-kernel plan: per-row populations and the row-aligned 32-particle items
     uint32_t* row_count = nullptr;
     size_t rows_cap = 0;
-    int2* items = nullptr;       // (first sorted index, particles) per item
+    Item* items = nullptr;       // row-aligned items of the force kernel
     size_t items_cap = 0;
     int* n_items = nullptr;
     // tiled CSR build: arrival slot per particle, per-tile totals
@@ -238,10 +247,10 @@ cudaError_t launch_cell_bounds(const uint32_t* keys, const uint32_t* vals, int n
                                uint32_t* end, int cells, float4* pos_sorted, cudaStream_t st);
 cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
                               const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
-                              const int2* items, const int* n_items, int max_items, float4* pos, float4* vel,
+                              const Item* items, const int* n_items, int max_items, float4* pos, float4* vel,
                               float4* acc, int* counts, cudaStream_t st);
 // Row-aligned items of at most 32 sorted particles (one cell row each).
-cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, int2* items, int* n_items,
+cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, Item* items, int* n_items,
                              cudaStream_t st);
 int max_step_items(int n, const Grid& g);
 int step_launches(int n);
@@ -257,7 +266,7 @@ int cell_list_launches(int n, int key_bits);
 // kernel's row-aligned items.  Rows of at most kTileCellsMax cells take the
 // tiled path (5 kernels); longer rows a radix sort.
 cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
-                                 Scratch& s, uint32_t* cell_off, int2* items, int* n_items, int* err, int* which,
+                                 Scratch& s, uint32_t* cell_off, Item* items, int* n_items, int* err, int* which,
                                  cudaStream_t st);
 int cell_list_csr_launches(int n, const Grid& g, bool with_plan);
 int cell_list_tiles(const Grid& g);  // 0 when the rows are longer than a tile

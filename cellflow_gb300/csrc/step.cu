@@ -80,6 +80,14 @@ __device__ __forceinline__ float staged_shift(float staged, float raw, float ext
 
 __device__ __forceinline__ int wrap_index(int v, int m) { return v < 0 ? v + m : (v >= m ? v - m : v); }
 
+// fmodf(x, W) of the integrator's wrap (ParticleSimulation.cu:159-161), exact:
+// for x in [0, 2W) it is x or x - W, and x - W is exact there (Sterbenz).
+__device__ __forceinline__ float wrap_pos(float x, float W)
+{
+    if (x >= 0.0f && x < 2.0f * W) return x >= W ? __fsub_rn(x, W) : x;
+    return fmodf(x, W);
+}
+
 // Staging origin on one axis for stencil cells [clo, chi] (shifted cell
 // coordinates, cell size cs) and the radius r of the box around it.  The
 // centre is used only where it is at least twice the half-width: then every
@@ -228,7 +236,7 @@ template <int kStage, int kMinBlocks, bool kGeneric, bool kUniformR>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
     step_force_kernel(StepConsts c, const PairTables* __restrict__ tables, const float4* __restrict__ pos_sorted,
                       const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ vals_sorted,
-                      const uint32_t* __restrict__ cell_off, const int2* __restrict__ items,
+                      const uint32_t* __restrict__ cell_off, const Item* __restrict__ items,
                       const int* __restrict__ n_items, float4* __restrict__ pos, float4* __restrict__ vel,
                       float4* __restrict__ acc, int* __restrict__ counts)
 {
@@ -278,27 +286,24 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     float2* wcoef = coef_base + (one_world ? 0 : warp * T * T);
     const float* xyf = reinterpret_cast<const float*>(w.xy);
     const float* zcf = reinterpret_cast<const float*>(w.zc);
-    const int2 it = items[item];
-    const bool active = lane < it.y;
-    const int t = it.x + (active ? lane : 0);
+    const Item it = items[item];
+    const bool active = lane < it.count;
+    const int t = it.first + (active ? lane : 0);
     Lane L;
     L.h = pos_sorted[t];
     L.tp = __float_as_uint(L.h.w) & kTypeMask;
     L.fx = L.fy = L.fz = 0.0f;
     L.count = 0;
 
-    // cell coordinates inside the item's world (items never straddle worlds)
+    // cell coordinates inside the item's world (items never straddle worlds or rows)
     const int mx = c.grid.m[0], my = c.grid.m[1], mz = c.grid.m[2];
-    const uint32_t cells_w = (uint32_t)c.grid.cells_w;
-    const uint32_t key_first = keys_sorted[it.x];
-    const uint32_t world = key_first / cells_w;
-    const uint32_t world_base = world * cells_w;
-    const uint32_t local_first = key_first - world_base;
-    const int x0 = (int)(local_first % (uint32_t)mx);
-    const int x1 = (int)((keys_sorted[it.x + it.y - 1] - world_base) % (uint32_t)mx);
-    const int yc = (int)((local_first / (uint32_t)mx) % (uint32_t)my);
-    const int zc = (int)(local_first / (uint32_t)(mx * my));
-    const int hx = (int)((keys_sorted[t] - world_base) % (uint32_t)mx);
+    const uint32_t world = (uint32_t)it.world;
+    const uint32_t world_base = world * (uint32_t)c.grid.cells_w;
+    const int yc = it.yz & 0xffff, zc = it.yz >> 16;
+    const uint32_t row_base = world_base + (uint32_t)((zc * my + yc) * mx);
+    const int x0 = (int)(keys_sorted[it.first] - row_base);
+    const int x1 = (int)(keys_sorted[it.first + it.count - 1] - row_base);
+    const int hx = (int)(keys_sorted[t] - row_base);
     if (!one_world) {
         for (int e = lane; e < T * T; e += 32) {
             const int a = e / T, b = e - a * T;
@@ -322,7 +327,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         // +kFar padding slots
         const float hxf = mine ? L.h.x : -kFar, hyf = mine ? L.h.y : -kFar, hzf = mine ? L.h.z : -kFar;
 
-        // segments: lane 2*row + half describes one contiguous range of the snapshot
         const int xlo = mx > 1 ? px0 - 1 : 0;
         const int xhi = mx > 1 ? min(px1 + 1, xlo + mx - 1) : 0;  // inclusive, at most mx cells
 
@@ -357,16 +361,18 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         } else {
             H.m2x = H.m2y = H.m2z = H.k = make_float2(0.0f, 0.0f);
         }
+        // segments: lane 2*row + half describes one contiguous range of the snapshot and
+        // its periodic shift less the origin (zero on generic grids)
         int seg_beg = 0, seg_len = 0;
-        uint32_t seg_code = 0;
+        float seg_sx = 0.0f, seg_sy = 0.0f, seg_sz = 0.0f;
         const int ny = my > 1 ? 3 : 1, nz = mz > 1 ? 3 : 1;
         const int nseg = 2 * ny * nz;
         {
             const int row = lane >> 1, half = lane & 1;
-            const int oy = ny > 1 ? (row % ny) - 1 : 0, oz = nz > 1 ? (row / ny) - 1 : 0;
-            const int yy = wrap_index(yc + oy, my), zz = wrap_index(zc + oz, mz);
-            const uint32_t cy = (yc + oy < 0) ? 1u : (yc + oy >= my ? 2u : 0u);
-            const uint32_t cz = (zc + oz < 0) ? 1u : (zc + oz >= mz ? 2u : 0u);
+            const int dy_row = ny > 1 ? (row % ny) - 1 : 0, dz_row = nz > 1 ? (row / ny) - 1 : 0;
+            const int yy = wrap_index(yc + dy_row, my), zz = wrap_index(zc + dz_row, mz);
+            const uint32_t cy = (yc + dy_row < 0) ? 1u : (yc + dy_row >= my ? 2u : 0u);
+            const uint32_t cz = (zc + dz_row < 0) ? 1u : (zc + dz_row >= mz ? 2u : 0u);
             // split [xlo, xhi] at the box edge: half 0 is the in-box part, half 1 the wrapped part
             int a = xlo, b = xhi;
             uint32_t cx = 0u;
@@ -383,7 +389,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 const uint32_t base = world_base + (uint32_t)((zz * my + yy) * mx);
                 seg_beg = (int)cell_off[base + a];
                 seg_len = (int)cell_off[base + b + 1] - seg_beg;
-                seg_code = kGeneric ? 0u : (cx | (cy << 2) | (cz << 4));
+                if (!kGeneric) {
+                    seg_sx = code_shift(cx, c.ext[0]) - ox;
+                    seg_sy = code_shift(cy, c.ext[1]) - oy;
+                    seg_sz = code_shift(cz, c.ext[2]) - oz;
+                }
             }
         }
         int seg_pre = seg_len;
@@ -394,29 +404,34 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         }
         const int total = __shfl_sync(0xffffffffu, seg_pre, 31);
         seg_pre -= seg_len;
+        // the home's place in the concatenation: its cell is in the centre row's in-box part
+        const int seg_c = 2 * ((nz > 1 ? ny : 0) + (ny > 1 ? 1 : 0));
+        const int beg_c = __shfl_sync(0xffffffffu, seg_beg, seg_c);
+        const int len_c = __shfl_sync(0xffffffffu, seg_len, seg_c);
+        const int pre_c = __shfl_sync(0xffffffffu, seg_pre, seg_c);
+        const int g_own = (t >= beg_c && t < beg_c + len_c) ? pre_c + (t - beg_c) : -1;
 
         const int share_lo = (int)((long long)total * part / split);
         const int share_hi = (int)((long long)total * (part + 1) / split);
         for (int base = share_lo; base < share_hi; base += kStage) {
             const int lim = min(kStage, share_hi - base);
             const int ngroups = (lim + 31) >> 5;
-            int own = -1;  // this lane's own slot in the batch (self exclusion)
-            // ---- stage [base, base + lim) of the concatenated segments
-            for (int sg = 0; sg < nseg; sg++) {
+            // this lane's own slot in the batch (self exclusion), -1 when elsewhere
+            const int own = (g_own >= base && g_own < base + lim) ? g_own - base : -1;
+            // ---- stage [base, base + lim) of the concatenated segments: only the segments
+            // that overlap it (a warp-uniform ballot over the segment lanes)
+            uint32_t overlap = __ballot_sync(0xffffffffu, lane < nseg && seg_len > 0 && seg_pre < base + lim &&
+                                                              seg_pre + seg_len > base);
+            while (overlap) {
+                const int sg = __ffs(overlap) - 1;
+                overlap &= overlap - 1u;
                 const int pre = __shfl_sync(0xffffffffu, seg_pre, sg);
                 const int len = __shfl_sync(0xffffffffu, seg_len, sg);
                 const int beg = __shfl_sync(0xffffffffu, seg_beg, sg);
-                const uint32_t code = __shfl_sync(0xffffffffu, seg_code, sg);
-                if (t >= beg && t < beg + len) {
-                    const int g = pre + (t - beg);
-                    if (g >= base && g < base + lim) own = g - base;
-                }
+                const float sx = __shfl_sync(0xffffffffu, seg_sx, sg);
+                const float sy = __shfl_sync(0xffffffffu, seg_sy, sg);
+                const float sz = __shfl_sync(0xffffffffu, seg_sz, sg);
                 const int lo = max(pre, base), hi = min(pre + len, base + lim);
-                if (hi <= lo) continue;
-                // periodic shift less the origin (both zero on generic grids)
-                const float sx = code_shift(code & 3u, c.ext[0]) - ox;
-                const float sy = code_shift((code >> 2) & 3u, c.ext[1]) - oy;
-                const float sz = code_shift(code >> 4, c.ext[2]) - oz;
                 for (int g = lo + lane; g < hi; g += 32) {
                     const int slot = g - base;
                     const int j = beg + (g - pre);
@@ -576,9 +591,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     float px = __fadd_rn(L.h.x, __fmul_rn(vx, c.delta_t));
     float py = __fadd_rn(L.h.y, __fmul_rn(vy, c.delta_t));
     float pz = __fadd_rn(L.h.z, __fmul_rn(vz, c.delta_t));
-    px = fmodf(__fadd_rn(px, c.ext[0]), c.ext[0]);
-    py = fmodf(__fadd_rn(py, c.ext[1]), c.ext[1]);
-    pz = fmodf(__fadd_rn(pz, c.ext[2]), c.ext[2]);
+    px = wrap_pos(__fadd_rn(px, c.ext[0]), c.ext[0]);
+    py = wrap_pos(__fadd_rn(py, c.ext[1]), c.ext[1]);
+    pz = wrap_pos(__fadd_rn(pz, c.ext[2]), c.ext[2]);
     pos[i] = make_float4(px, py, pz, L.h.w);
     vel[i] = make_float4(vx, vy, vz, 0.0f);
     acc[i] = make_float4(fx, fy, fz, 0.0f);
@@ -588,7 +603,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 // Items: each row of cells (rows = (y, z) pairs) cut into chunks of at most
 // 32 sorted particles.  One block; rows are split into contiguous segments.
 __global__ void __launch_bounds__(1024)
-    plan_kernel(const uint32_t* __restrict__ cell_off, int mx, int rows, int2* __restrict__ items,
+    plan_kernel(const uint32_t* __restrict__ cell_off, int mx, int my, int mz, int rows, Item* __restrict__ items,
                 int* __restrict__ n_items)
 {
     __shared__ uint32_t s_chunk[1024];
@@ -612,7 +627,9 @@ __global__ void __launch_bounds__(1024)
     for (int r = r0; r < r1; r++) {
         const uint32_t start = cell_off[r * mx];
         const uint32_t cnt = cell_off[(r + 1) * mx] - start;
-        for (uint32_t k = 0; k < cnt; k += 32u) items[item++] = make_int2((int)(start + k), (int)min(32u, cnt - k));
+        const int yz_w = r / my;
+        const int yz = (r - yz_w * my) | ((yz_w % mz) << 16), world = yz_w / mz;
+        for (uint32_t k = 0; k < cnt; k += 32u) items[item++] = Item{(int)(start + k), (int)min(32u, cnt - k), yz, world};
     }
     if (tid == 1023) *n_items = (int)s_chunk[1023];
 }
@@ -639,7 +656,7 @@ cudaError_t configure_variant()
 template <int S, int B>
 cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
                            const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
-                           const int2* items, const int* n_items, int blocks, float4* pos, float4* vel, float4* acc,
+                           const Item* items, const int* n_items, int blocks, float4* pos, float4* vel, float4* acc,
                            int* counts, cudaStream_t st)
 {
     // staging per warp; force coefficients per block (one world) or per warp (a batch)
@@ -669,11 +686,11 @@ int max_step_items(int n, const Grid& g) { return (n + 31) / 32 + g.worlds * g.m
 
 int step_launches(int n) { return n > 0 ? 1 : 0; }  // the force kernel (the plan is part of the cell list)
 
-cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, int2* items, int* n_items,
+cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, Item* items, int* n_items,
                              cudaStream_t st)
 {
     if (n <= 0) return cudaMemsetAsync(n_items, 0, sizeof(int), st);
-    plan_kernel<<<1, 1024, 0, st>>>(cell_off, g.m[0], g.worlds * g.m[1] * g.m[2], items, n_items);
+    plan_kernel<<<1, 1024, 0, st>>>(cell_off, g.m[0], g.m[1], g.m[2], g.worlds * g.m[1] * g.m[2], items, n_items);
     return cudaGetLastError();
 }
 
@@ -690,7 +707,7 @@ cudaError_t configure_step_force()
 
 cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
                               const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
-                              const int2* items, const int* n_items, int max_items, float4* pos, float4* vel,
+                              const Item* items, const int* n_items, int max_items, float4* pos, float4* vel,
                               float4* acc, int* counts, cudaStream_t st)
 {
     if (c.n <= 0 || max_items <= 0) return cudaSuccess;
