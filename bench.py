@@ -107,6 +107,20 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
 
 
+def profiled_traffic(workload: str):
+    """DRAM bytes (read + write) of one force-kernel launch on this workload from the committed
+    ncu summary (a `traffic_bytes_per_launch WORKLOAD BYTES` line), or None."""
+    f = ROOT / "profiles" / "step_force_kernel_plain_n100k_blobs_n1m.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        parts = line.split()
+        if len(parts) == 3 and parts[0] == "traffic_bytes_per_launch" and parts[1] == workload:
+            return {"bytes_per_launch": int(parts[2]), "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                    "profiles/step_force_kernel_plain_n100k_blobs_n1m.md"}
+    return None
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -403,7 +417,9 @@ def run_gb300(args, rank, world, local):
                 "work_model": "9*C27 + 17*I + 25*N flops per step",
                 "c27_per_particle_step": c27_total / (w.n * args.steps),
                 "interacting_per_particle_step": inter_total / (w.n * args.steps),
-                "traffic": None,
+                "traffic": (profiled_traffic(w.name) or {}).get("bytes_per_launch"),
+                "traffic_unit": "bytes per launch (one ncu capture of this workload's force kernel)",
+                "traffic_source": (profiled_traffic(w.name) or {}).get("source"),
             },
             "roofline_cell_list": {
                 "bound": "hbm", "achieved": cell_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
