@@ -11,7 +11,9 @@ Tolerances (FP32, one step, library vs the reference's FP32 step):
                approximations move the result by a few ulp of those
                quantities, never of the (possibly cancelled) result.
   velocity     |v - v_ref| <= 1e-5 * (|v_ref| + dt * m_i)
-  position     minimum-image |p - p_ref| <= 1e-5 * |p_ref| + 2 ulp(extent)
+  position     minimum-image |p - p_ref| <= 1e-5 * |p_ref| + 2 ulp(extent) + dt * (velocity
+               tolerance): the position is p + v dt, so the velocity's allowed error
+               carries over (it matters where thousands of large terms nearly cancel)
 """
 
 from __future__ import annotations
@@ -42,7 +44,7 @@ def check_step(rec, ref_pos, ref_vel, ref_acc, mag, dt, extent, label=""):
     vtol = REL * (np.abs(ref_vel) + dt * np.asarray(mag)[:, None]) + 1e-30
     e_vel = (np.abs(vel - ref_vel) / vtol).max() if len(vel) else 0.0
     assert e_vel <= 1.0, f"{label} velocity error {e_vel:.3e} of tolerance"
-    ptol = REL * np.abs(np.asarray(ref_pos, np.float64)) + 2 * np.spacing(np.float32(extent))
+    ptol = REL * np.abs(np.asarray(ref_pos, np.float64)) + 2 * np.spacing(np.float32(extent)) + dt * vtol
     dpos = np.abs(min_image(pos - ref_pos, extent))
     e_pos = (dpos / ptol).max() if len(pos) else 0.0
     assert e_pos <= 1.0, f"{label} position error {e_pos:.3e} of tolerance"
