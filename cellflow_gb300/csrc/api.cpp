@@ -364,19 +364,6 @@ int check_params(const cf_world* w, const cf_step_params* p)
     return CF_OK;
 }
 
-// Host-side cell list: hash, stable radix sort, start/end and sorted snapshot.
-// Returns the buffer index that holds the sorted keys and values.
-int build_cell_list(cf_world* w, const Grid& g, const float* ext, int* which)
-{
-    Scratch& s = w->s;
-    int rc = ensure_cells(w, g.cells);
-    if (rc) return rc;
-    CF_CUDA(launch_cell_hash(w->pos, w->n, g, ext, w->num_types, s.keys[0], w->err, w->stream));
-    CF_CUDA(launch_radix_sort(s, w->n, g.key_bits, which, w->stream));
-    CF_CUDA(launch_cell_bounds(s.keys[*which], s.vals[*which], w->n, w->pos, s.cell_start, s.cell_end, g.cells,
-                               s.pos_sorted, w->stream));
-    return CF_OK;
-}
 
 // Bound below which the force kernel's contracted squared distance proves the
 // exact test passes: d2a < bound  implies  fl(d2e + 1e-4) < t, with the same
@@ -1285,13 +1272,16 @@ int proximity_enqueue(cf_world* w, float distance, int max_conn)
     int rc = ensure_prox(w);
     if (rc) return rc;
     Grid g = choose_prox_grid(w->ext, distance, kMaxCells);
-    int which = 0;
-    rc = build_cell_list(w, g, w->ext, &which);
+    rc = ensure_offsets(w, g.cells);
     if (rc) return rc;
     Scratch& s = w->s;
+    // the step's tiled cell list on the proximity grid: cell c holds cell_off[c] .. cell_off[c + 1]
+    int which = 0;
+    CF_CUDA(launch_cell_list_csr(w->pos, w->n, g, w->ext, w->num_types, s, s.cell_off, nullptr, nullptr, w->err,
+                                 &which, w->stream));
     const float dsq = distance * distance;  // ParticleSimulation.cu:660
     CF_CUDA(cudaMemsetAsync(s.prox_count + w->n, 0, sizeof(uint32_t), w->stream));
-    CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_start, s.cell_end, g, w->n,
+    CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.cell_off + 1, g, w->n,
                                     dsq, max_conn, s.prox_slots, s.prox_count, w->stream));
     CF_CUDA(launch_scan_exclusive(s.prox_count, s.prox_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
     CF_CUDA(cudaMemcpyAsync(&w->host_words[1], s.prox_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost,
@@ -1314,12 +1304,14 @@ int mesh_enqueue(cf_world* w, float distance, int max_conn)
     const float hysteresis = 1.2f;
     const float dsq = distance * distance * (hysteresis * hysteresis);
     Grid g = choose_prox_grid(w->ext, nextafterf(std::sqrt(dsq), INFINITY), kMaxCells);
-    int which = 0;
-    rc = build_cell_list(w, g, w->ext, &which);
+    rc = ensure_offsets(w, g.cells);
     if (rc) return rc;
     Scratch& s = w->s;
+    int which = 0;
+    CF_CUDA(launch_cell_list_csr(w->pos, w->n, g, w->ext, w->num_types, s, s.cell_off, nullptr, nullptr, w->err,
+                                 &which, w->stream));
     CF_CUDA(cudaMemsetAsync(s.mesh_count + w->n, 0, sizeof(uint32_t), w->stream));
-    CF_CUDA(launch_mesh_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_start, s.cell_end, g, w->n, dsq,
+    CF_CUDA(launch_mesh_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.cell_off + 1, g, w->n, dsq,
                                std::min(max_conn, CF_MESH_MAX_CONN), s.mesh_slots, s.mesh_count, w->stream));
     CF_CUDA(launch_scan_exclusive(s.mesh_count, s.mesh_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
     CF_CUDA(cudaMemcpyAsync(&w->host_words[1], s.mesh_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost,
