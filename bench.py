@@ -50,6 +50,11 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--prox-calls", type=int, default=50, help="proximity-graph calls timed (workloads with a distance)")
+    ap.add_argument("--profile-steps", type=int, default=None, metavar="S",
+                    help="no timing: step the workload's world S times with --variant and exit (a short, "
+                         "fixed launch sequence for ncu captures)")
+    ap.add_argument("--variant", type=int, default=None, help="force-kernel variant for --profile-steps "
+                    "(default: the autotuner's pick)")
     return ap.parse_args()
 
 
@@ -107,18 +112,28 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
 
 
-def profiled_traffic(workload: str):
-    """DRAM bytes (read + write) of one force-kernel launch on this workload from the committed
-    ncu summary (a `traffic_bytes_per_launch WORKLOAD BYTES` line), or None."""
-    f = ROOT / "profiles" / "step_force_kernel_plain_n100k_blobs_n1m.md"
+FORCE_PROFILE = "profiles/step_force_kernel_plain_n100k_blobs_n1m.md"
+
+
+def profile_figure(key: str, workload: str):
+    """A figure of the committed ncu summary of the force kernel: its `KEY WORKLOAD VALUE` line, or None."""
+    f = ROOT / FORCE_PROFILE
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
         parts = line.split()
-        if len(parts) == 3 and parts[0] == "traffic_bytes_per_launch" and parts[1] == workload:
-            return {"bytes_per_launch": int(parts[2]), "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                    "profiles/step_force_kernel_plain_n100k_blobs_n1m.md"}
+        if len(parts) == 3 and parts[0] == key and parts[1] == workload:
+            return float(parts[2])
     return None
+
+
+def profiled_traffic(workload: str):
+    """DRAM bytes (read + write) of one force-kernel launch on this workload from the committed
+    ncu summary (a `traffic_bytes_per_launch WORKLOAD BYTES` line), or None."""
+    v = profile_figure("traffic_bytes_per_launch", workload)
+    if v is None:
+        return None
+    return {"bytes_per_launch": int(v), "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, " + FORCE_PROFILE}
 
 
 def dist_env():
@@ -181,8 +196,31 @@ def cpu_reference_sample(w, params, pos, types, table, radio, budget_s: float):
     stride = max(1, w.n // rows_target)
     dt, r = run((0, w.n, stride))
     desc = (f"{r} of {w.n} particles (every {stride}th), each against all {w.n}, one step from the initial "
-            f"state; {cores} OpenMP threads; {dt:.2f} s")
+            f"state; {cores} OpenMP threads; {dt:.2f} s"
+            + ("" if stride == 1 else "; rate extrapolated from the strided sample (each sampled row costs a full row)"))
     return r / dt, kind, cores, desc
+
+
+def host_cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            key, _, val = line.partition(":")
+            if key.strip() == "Model name" and val.strip():
+                return val.strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            key, _, val = line.partition(":")
+            if key.strip().lower() in ("model name", "cpu model", "processor name") and val.strip():
+                return val.strip()
+        import platform
+
+        return platform.processor() or platform.machine()
+    except OSError:
+        return "unknown"
 
 
 def run_reference_arm(args, rank, world):
@@ -273,6 +311,7 @@ def run_reference_arm(args, rank, world):
         "dtype": "f32", "data": "synthetic (seeded Philox), see config",
         "config": config,
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": kind,
+                         "cpu_model": host_cpu_model(),
                          "sample": sample},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -401,7 +440,8 @@ def run_gb300(args, rank, world, local):
         cpu = None
         if not args.no_cpu_baseline:
             v, kind, cores, desc = cpu_reference_sample(w, params, pos, types, table, radio, args.cpu_seconds)
-            cpu = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": kind, "sample": desc}
+            cpu = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": kind, "sample": desc,
+                   "cpu_model": host_cpu_model()}
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
@@ -420,6 +460,8 @@ def run_gb300(args, rank, world, local):
                 "traffic": (profiled_traffic(w.name) or {}).get("bytes_per_launch"),
                 "traffic_unit": "bytes per launch (one ncu capture of this workload's force kernel)",
                 "traffic_source": (profiled_traffic(w.name) or {}).get("source"),
+                "ncu_fma_pipe_pct": profile_figure("fma_pipe_inst_pct", w.name),
+                "ncu_issue_active_pct": profile_figure("issue_active_pct", w.name),
             },
             "roofline_cell_list": {
                 "bound": "hbm", "achieved": cell_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
@@ -740,9 +782,15 @@ def proximity_timing(sim, w, stream, calls):
     for _ in range(calls):
         host_edges = sim.proximity_edges(dist, mc)
     host_s = (time.perf_counter() - t0) / calls
+    peaks = measured_peaks()
+    prox_bytes = 16 * n + 8 * int(edges)
     out = {
         "distance": dist, "max_conn": mc, "edges": int(edges), "calls": calls,
         "value": edges / dev_s, "unit": "edges/s", "ms_per_call": dev_s * 1e3,
+        "roofline": {"bound": "hbm", "achieved": prox_bytes / dev_s / 1e9, "peak": peaks.get("hbm_gbs"),
+                     "unit": "GB/s", "frac": prox_bytes / dev_s / 1e9 / peaks.get("hbm_gbs", 6800.0),
+                     "work_model": "16 B/particle + 8 B/edge per call (the call is latency-bound: ~10 small "
+                                   "kernels and a count read-back)"},
         "path": "cf_proximity_vertices_device (device VBO, count read back; synchronising, as the reference)",
         "host_edges": {"value": len(host_edges) / host_s, "unit": "edges/s", "ms_per_call": host_s * 1e3,
                        "path": "cf_proximity_edges (int32 pairs into host memory)"},
@@ -828,9 +876,34 @@ def reference_gpu_kernel(w, params, pos, types, table, radio, stream):
             "note": "reference O(N^2) kernel, in place (racy as in the reference), <<<ceil(N/256),256>>>"}
 
 
+def profile_steps(args) -> None:
+    """--profile-steps S: S plain steps of the workload from its initial state under one force-kernel
+    variant, nothing timed, for an ncu capture of step k with `-k regex:step_force_kernel -s k-1 -c 1`."""
+    import numpy as np
+
+    from cellflow_gb300 import inputs
+    from cellflow_gb300.world import ParticleSimulation
+
+    w = inputs.WORKLOADS[args.workload]
+    params = w.params()
+    sim = ParticleSimulation(w.n, w.num_types, w.extent, w.extent, w.extent)
+    sim.set_particles(w.positions(), w.types())
+    sim.setForceTable(w.table())
+    sim.setRadioByType(np.zeros(w.num_types, np.float32))
+    if args.variant is not None:
+        sim.set_force_variant(args.variant)
+    sim.simulate(params, args.profile_steps)
+    sim.sync()
+    sim.close()
+    print(json.dumps({"profile_steps": args.profile_steps, "workload": w.name, "variant": args.variant}))
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
+    if args.profile_steps is not None:
+        profile_steps(args)
+        return
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
         return
