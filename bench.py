@@ -412,21 +412,38 @@ def run_gb300(args, rank, world, local):
     sim.set_state(*state0)
     host_np[:] = sim.getParticleData()
     hp = C.c_void_p(host.data_ptr())
-    for _ in range(3):
-        _lib.check(lib.cf_set_particles(sim.handle, hp, w.n), "cf_set_particles")
-        sim.simulate(params, 1)
-        _lib.check(lib.cf_get_particles(sim.handle, hp, w.n), "cf_get_particles")
-    barrier()
-    e2e_wall = 0.0
-    for _ in range(e2e_steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        _lib.check(lib.cf_set_particles(sim.handle, hp, w.n), "cf_set_particles")
-        sim.simulate(params, 1)
-        _lib.check(lib.cf_get_particles(sim.handle, hp, w.n), "cf_get_particles")
-        e2e_wall += time.perf_counter() - t0
+    pc = params.to_c()
+
+    def e2e_run(one_call: bool) -> float:
+        """Host wall time of e2e_steps steps, each uploading the pinned AoS records, stepping and
+        reading them back; L2 flushed before each step, outside the timed span."""
+        def step():
+            if one_call:
+                _lib.check(lib.cf_step_host(sim.handle, C.byref(pc), hp, hp, w.n), "cf_step_host")
+            else:
+                _lib.check(lib.cf_set_particles(sim.handle, hp, w.n), "cf_set_particles")
+                sim.simulate(params, 1)
+                _lib.check(lib.cf_get_particles(sim.handle, hp, w.n), "cf_get_particles")
+
+        for _ in range(3):
+            step()
+        barrier()
+        total = 0.0
+        for _ in range(e2e_steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            step()
+            total += time.perf_counter() - t0
+        return total
+
+    sim.set_state(*state0)
+    host_np[:] = sim.getParticleData()
+    e2e_three_wall = e2e_run(False)
+    sim.set_state(*state0)
+    host_np[:] = sim.getParticleData()
+    e2e_wall = e2e_run(True)
     e2e_value = w.n * e2e_steps * world / e2e_wall
 
     # ---- reference kernel on this GPU (its O(N^2) kernel built for sm_103a), a few steps
@@ -472,7 +489,9 @@ def run_gb300(args, rank, world, local):
             "phase_ms_per_step": {"cell_list": prof.cell_list_ms / args.steps, "force": prof.force_ms / args.steps},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": w.n * 44,
                     "d2h_bytes_per_step": w.n * 44, "steps": e2e_steps,
-                    "path": "cf_set_particles (pinned AoS) + cf_step + cf_get_particles"},
+                    "path": "cf_step_host: pinned 44-B AoS records up, one step, records back (one CUDA graph)",
+                    "three_calls": {"value": w.n * e2e_steps * world / e2e_three_wall, "unit": "particle-steps/s",
+                                    "path": "cf_set_particles + cf_step + cf_get_particles"}},
             "gpu_launches": int(prof.launches),
             "clocks": clk,
             "wall_s_timed_region": wall,

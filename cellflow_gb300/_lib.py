@@ -172,6 +172,7 @@ _SIGNATURES = {
     "cf_rotate_radio_by_type": (C.c_int, [_W]),
     "cf_lfo_ratio": (C.c_float, [C.c_float, C.c_float, C.c_float, C.c_float]),
     "cf_step": (C.c_int, [_W, _P(StepParams), C.c_int]),
+    "cf_step_host": (C.c_int, [_W, _P(StepParams), C.c_void_p, C.c_void_p, C.c_int]),
     "cf_get_grid": (C.c_int, [_W, _P(StepParams), _P(GridInfo)]),
     "cf_autotune_step": (C.c_int, [_W, _P(StepParams), C.c_int, _P(C.c_int)]),
     "cf_set_force_variant": (C.c_int, [_W, C.c_int]),

@@ -226,6 +226,13 @@ struct cf_world {
     int batch_graph_steps = 0;
     long long batch_graph_kernels = 0;  // kernel nodes of the captured graph
     cf::Rollout ro;
+    // cf_step_host: upload, step and read-back as one graph, keyed by the step
+    // constants, the host buffers and the scratch identity
+    cudaGraphExec_t host_graph = nullptr;
+    cf::StepConsts host_key;
+    const void* host_in = nullptr;
+    void* host_out = nullptr;
+    const void* host_bufs = nullptr;
 };
 
 namespace cf {

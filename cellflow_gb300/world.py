@@ -118,6 +118,16 @@ class ParticleSimulation:
         check(self._lib.cf_get_particles(self._h, _ptr(out), n), "cf_get_particles")
         return out
 
+    def step_host(self, params: SimulationParams, records_in, records_out=None) -> np.ndarray:
+        """One step with host buffers (cf_step_host): upload `records_in` (AoS, the reference
+        layout), step, read back into `records_out` (default: a new array).  Page-locked
+        buffers (e.g. numpy views of pinned torch tensors) run as one CUDA graph."""
+        rin = np.ascontiguousarray(records_in, dtype=PARTICLE_DTYPE)
+        out = np.zeros(len(rin), dtype=PARTICLE_DTYPE) if records_out is None else records_out
+        p = params.to_c()
+        check(self._lib.cf_step_host(self._h, C.byref(p), _ptr(rin), _ptr(out), len(rin)), "cf_step_host")
+        return out
+
     def setParticleData(self, records: np.ndarray) -> None:
         rec = np.ascontiguousarray(records, dtype=PARTICLE_DTYPE)
         check(self._lib.cf_set_particles(self._h, _ptr(rec), len(rec)), "cf_set_particles")

@@ -180,6 +180,16 @@ float cf_lfo_ratio(float ratio, float lfo_a, float lfo_s, float t_seconds);
  * builds the cell list, computes forces, neighbour counts and the
  * density-adaptive scale, integrates and wraps.  Asynchronous. */
 int cf_step(cf_world* w, const cf_step_params* p, int nsteps);
+/* One step with host buffers, for a caller that keeps the particles in host
+ * memory: uploads the 44-B records from `in`, steps once (as cf_step), and
+ * writes the records to `out`; synchronises and reports device errors.
+ * Equivalent to cf_set_particles + cf_step + cf_get_particles.  When `in` and
+ * `out` are page-locked (cudaHostAlloc / cudaHostRegister) the copies and
+ * kernels run as one cached CUDA graph; otherwise as the three calls.  `in`
+ * and `out` may be the same buffer.  No counterpart in the reference (its
+ * state stays on the device and only getParticleData copies it back). */
+int cf_step_host(cf_world* w, const cf_step_params* p, const cf_particle* in, cf_particle* out, int n);
+
 /* Force-kernel variants: v % 4 picks the staging: 0 = 256 candidates staged
  * per warp batch, register budget for 8 blocks per SM; 1 = 256 staged, 6
  * blocks per SM; 2 = 512 staged, 4 blocks per SM; 3 = 384 staged, 6 blocks

@@ -80,6 +80,12 @@ public:
         particles.resize(getParticleCount());
         check(cf_get_particles(w_, particles.data(), (int)particles.size()));
     }
+    // One step from and to host records (upload, step, read back); one CUDA graph
+    // when both buffers are page-locked.
+    void simulateHost(const cf_step_params& params, const Particle* in, Particle* out)
+    {
+        check(cf_step_host(w_, &params, in, out, getParticleCount()));
+    }
     void setParticleCount(int count) { check(cf_set_particle_count(w_, count, ++seed_)); }
     int getParticleCount() const
     {
