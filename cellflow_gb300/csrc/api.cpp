@@ -177,8 +177,9 @@ int ensure_offsets(cf_world* w, int cells)
 {
     Scratch& s = w->s;
     const size_t need_tmp = scan_tmp_entries(cells + 1);
-    // tiles of the CSR build: every tile holds more than kTileCellsMax / 2 cells
-    const size_t need_tiles = (size_t)cells / (kTileCellsMax / 2) + 2;
+    // tiles of the CSR build: at most 257 on grids spread thin, else every tile
+    // holds more than kTileCellsMax / 2 cells
+    const size_t need_tiles = (size_t)cells / (kTileCellsMax / 2) + 2 + 257;
     if ((size_t)cells + 1 <= s.off_cap && need_tmp <= s.scan_tmp_cap && need_tiles <= s.tiles_cap) return CF_OK;
     CF_CUDA(cudaStreamSynchronize(w->stream));
     drop_graphs(w);

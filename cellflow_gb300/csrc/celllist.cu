@@ -9,6 +9,8 @@
 // per-cell range are reproducible bit for bit.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "cf_internal.hpp"
 
 namespace cf {
@@ -266,12 +268,13 @@ __global__ void __launch_bounds__(kThreads)
 constexpr int kTileThreads = 512;
 constexpr int kTileItems = kTileCellsMax / kTileThreads;  // cells (and rows) per thread at most
 constexpr int kTileWarps = kTileThreads / 32;
+constexpr int kTileTarget = 256;  // tiles a grid is spread over at least, row count permitting
 
 struct TileGeom {
     int m0;             // cells per row
     int m1, m2;         // cells along y and z (a row r is y = r % m1, z = r / m1 % m2, world = r / (m1 m2))
     int rows;           // rows of the whole grid (all worlds)
-    int rows_per_tile;  // whole rows per tile: floor(kTileCellsMax / m0) >= 1
+    int rows_per_tile;  // whole rows per tile (tile_rows): 1 .. floor(kTileCellsMax / m0)
     int tiles;
 };
 
@@ -609,11 +612,21 @@ cudaError_t launch_cell_bounds(const uint32_t* keys, const uint32_t* vals, int n
 // Cell list in CSR form for the step: keys[0] = cell ids, radix-sorted
 // (keys, vals)[*which], cell_off[c] = particles in cells < c (cells + 1
 // entries), pos_sorted = positions in sorted order.
+// Whole rows per tile: as many as fit in kTileCellsMax cells, fewer when that
+// would leave under kTileTarget tiles (small grids: more blocks, shorter scans).
+int tile_rows(const Grid& g)
+{
+    const int rows = g.cells / g.m[0];
+    const int fit = kTileCellsMax / g.m[0];
+    const int spread = (rows + kTileTarget - 1) / kTileTarget;
+    return std::max(1, std::min(fit, spread));
+}
+
 int cell_list_tiles(const Grid& g)
 {
     if (g.m[0] > kTileCellsMax) return 0;
     const int rows = g.cells / g.m[0];
-    const int per = kTileCellsMax / g.m[0];
+    const int per = tile_rows(g);
     return (rows + per - 1) / per;
 }
 
@@ -641,7 +654,7 @@ cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const 
     tg.m1 = g.m[1];
     tg.m2 = g.m[2];
     tg.rows = g.cells / g.m[0];
-    tg.rows_per_tile = kTileCellsMax / g.m[0];
+    tg.rows_per_tile = tile_rows(g);
     tg.tiles = tiles;
     tile_reduce_kernel<<<tiles, kTileThreads, 0, st>>>(cell_off, tg, s.tile_sums);
     tile_apply_kernel<<<tiles, kTileThreads, 0, st>>>(cell_off, tg, s.tile_sums, items, n_items);
