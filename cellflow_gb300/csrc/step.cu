@@ -6,9 +6,13 @@
 // an item are the particles of the union of its homes' 27-cell stencils:
 // 9 rows, each a run of consecutive cells, i.e. one contiguous range of the
 // sorted snapshot (two where the run wraps around the box in x).  The warp
-// copies those ranges into shared memory, 256 or 512 at a time (chosen by
-// the autotuner), with their periodic shift already applied, and every lane
-// tests every staged candidate (broadcast reads).
+// copies those ranges into shared memory, 256, 384 or 512 at a time (chosen
+// by the autotuner), with their periodic shift already applied, and every
+// lane tests every staged candidate (broadcast reads).  For worlds too small
+// to fill the GPU, 2 or 4 warps share an item, each taking an equal share of
+// its candidates; the first adds the others' partial sums in a fixed order.
+// Items are 16-B records (first particle, count, the row's y/z, world)
+// written by the cell list, so no per-item integer division is needed.
 //
 // Coordinates are staged relative to an origin per pass (the centre of the
 // stencil box where that keeps c - o exact, else 0), periodic shift folded
