@@ -78,6 +78,10 @@ void drop_graphs(cf_world* w)
     if (w->host_graph) cudaGraphExecDestroy(w->host_graph);
     w->host_graph = nullptr;
     w->host_bufs = nullptr;
+    for (auto& sg : w->sel_graph) {
+        if (sg.exec) cudaGraphExecDestroy(sg.exec);
+        sg = SelGraph();
+    }
 }
 
 // (Re)allocate per-particle state and scratch for w->n particles.
@@ -1357,6 +1361,42 @@ namespace {
 // Proximity selection: cell list with the proximity grid, per-particle
 // edges, exclusive scan.  Enqueues only: offsets land in prox_count[0..n] and
 // the edge total in host_words[1] once the stream has reached this point.
+// Runs a selection pass through its cached graph (captured on first use and
+// whenever the grid, distance, limit, particle or type count changes; buffer
+// reallocations drop it), or directly when graphs are off.
+extern "C++" {
+template <typename Body>
+int run_selection(cf_world* w, int kind, const Grid& g, float dsq, int max_conn, Body body)
+{
+    if (!w->use_graphs || w->stream == nullptr) return body();
+    SelGraph& sg = w->sel_graph[kind];
+    if (!(sg.exec && std::memcmp(&sg.g, &g, sizeof(g)) == 0 && sg.dsq == dsq && sg.max_conn == max_conn &&
+          sg.n == w->n && sg.types == w->num_types)) {
+        if (sg.exec) cudaGraphExecDestroy(sg.exec);
+        sg = SelGraph();
+        cudaGraph_t graph = nullptr;
+        CF_CUDA(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = body();
+        cudaError_t e = cudaStreamEndCapture(w->stream, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&sg.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+        sg.g = g;
+        sg.dsq = dsq;
+        sg.max_conn = max_conn;
+        sg.n = w->n;
+        sg.types = w->num_types;
+    }
+    CF_CUDA(cudaGraphLaunch(sg.exec, w->stream));
+    return CF_OK;
+}
+}  // extern "C++"
+
 int proximity_enqueue(cf_world* w, float distance, int max_conn)
 {
     if (!(distance >= 0.0f) || !std::isfinite(distance)) return fail(CF_ERR_INVALID, "distance must be finite, >= 0");
@@ -1368,18 +1408,20 @@ int proximity_enqueue(cf_world* w, float distance, int max_conn)
     rc = ensure_offsets(w, g.cells);
     if (rc) return rc;
     Scratch& s = w->s;
-    // the step's tiled cell list on the proximity grid: cell c holds cell_off[c] .. cell_off[c + 1]
-    int which = 0;
-    CF_CUDA(launch_cell_list_csr(w->pos, w->n, g, w->ext, w->num_types, s, s.cell_off, nullptr, nullptr, w->err,
-                                 &which, w->stream));
     const float dsq = distance * distance;  // ParticleSimulation.cu:660
-    CF_CUDA(cudaMemsetAsync(s.prox_count + w->n, 0, sizeof(uint32_t), w->stream));
-    CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.cell_off + 1, g, w->n,
-                                    dsq, max_conn, s.prox_slots, s.prox_count, w->stream));
-    CF_CUDA(launch_scan_exclusive(s.prox_count, s.prox_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
-    CF_CUDA(cudaMemcpyAsync(&w->host_words[1], s.prox_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                            w->stream));
-    return CF_OK;
+    return run_selection(w, 0, g, dsq, max_conn, [&]() -> int {
+        // the step's tiled cell list on the proximity grid: cell c holds cell_off[c] .. cell_off[c + 1]
+        int which = 0;
+        CF_CUDA(launch_cell_list_csr(w->pos, w->n, g, w->ext, w->num_types, s, s.cell_off, nullptr, nullptr, w->err,
+                                     &which, w->stream));
+        CF_CUDA(cudaMemsetAsync(s.prox_count + w->n, 0, sizeof(uint32_t), w->stream));
+        CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.cell_off + 1, g,
+                                        w->n, dsq, max_conn, s.prox_slots, s.prox_count, w->stream));
+        CF_CUDA(launch_scan_exclusive(s.prox_count, s.prox_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
+        CF_CUDA(cudaMemcpyAsync(&w->host_words[1], s.prox_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                w->stream));
+        return CF_OK;
+    });
 }
 
 // Triangle selection: cell list on the proximity grid of the mesh distance,
@@ -1400,16 +1442,18 @@ int mesh_enqueue(cf_world* w, float distance, int max_conn)
     rc = ensure_offsets(w, g.cells);
     if (rc) return rc;
     Scratch& s = w->s;
-    int which = 0;
-    CF_CUDA(launch_cell_list_csr(w->pos, w->n, g, w->ext, w->num_types, s, s.cell_off, nullptr, nullptr, w->err,
-                                 &which, w->stream));
-    CF_CUDA(cudaMemsetAsync(s.mesh_count + w->n, 0, sizeof(uint32_t), w->stream));
-    CF_CUDA(launch_mesh_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.cell_off + 1, g, w->n, dsq,
-                               std::min(max_conn, CF_MESH_MAX_CONN), s.mesh_slots, s.mesh_count, w->stream));
-    CF_CUDA(launch_scan_exclusive(s.mesh_count, s.mesh_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
-    CF_CUDA(cudaMemcpyAsync(&w->host_words[1], s.mesh_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                            w->stream));
-    return CF_OK;
+    return run_selection(w, 1, g, dsq, max_conn, [&]() -> int {
+        int which = 0;
+        CF_CUDA(launch_cell_list_csr(w->pos, w->n, g, w->ext, w->num_types, s, s.cell_off, nullptr, nullptr, w->err,
+                                     &which, w->stream));
+        CF_CUDA(cudaMemsetAsync(s.mesh_count + w->n, 0, sizeof(uint32_t), w->stream));
+        CF_CUDA(launch_mesh_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.cell_off + 1, g, w->n,
+                                   dsq, std::min(max_conn, CF_MESH_MAX_CONN), s.mesh_slots, s.mesh_count, w->stream));
+        CF_CUDA(launch_scan_exclusive(s.mesh_count, s.mesh_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
+        CF_CUDA(cudaMemcpyAsync(&w->host_words[1], s.mesh_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                w->stream));
+        return CF_OK;
+    });
 }
 
 // Copy `entries` int32 of the staging buffer to host memory and wait.

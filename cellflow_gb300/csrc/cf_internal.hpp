@@ -174,6 +174,15 @@ struct Rollout {
 };
 constexpr int kGradAccEntries = kTableSize + 8;
 
+// A cached CUDA graph of a selection pass (0: proximity edges, 1: triangle
+// mesh): cell list on its grid, selection kernel, scan, count read-back.
+struct SelGraph {
+    cudaGraphExec_t exec = nullptr;
+    Grid g{};
+    float dsq = 0.0f;
+    int max_conn = -1, n = -1, types = -1;
+};
+
 }  // namespace cf
 
 struct cf_world {
@@ -233,6 +242,7 @@ struct cf_world {
     const void* host_in = nullptr;
     void* host_out = nullptr;
     const void* host_bufs = nullptr;
+    cf::SelGraph sel_graph[2];
 };
 
 namespace cf {
