@@ -101,3 +101,25 @@ def test_full_size_edges(cflib):
     sim.close()
     ref = oracle.proximity_edges(pos, types, w.prox_distance, w.prox_max_conn)
     assert np.array_equal(got, ref)
+
+
+def test_selection_graphs_follow_parameters_and_positions(cflib):
+    """The proximity and triangle-mesh passes run as cached graphs: alternating distances and
+    connection limits re-capture them, and after steps the cached graphs see the new
+    positions.  Every call is checked against the oracle."""
+    n, T = 6000, 3
+    w = inputs.Workload("prox_cache", n=n, num_types=T, radius=0.1, steps=1, seed=41)
+    sim = ParticleSimulation(n, T, 2.0, 2.0, 2.0)
+    sim.set_particles(w.positions(), w.types())
+    sim.setForceTable(w.table())
+    sim.setRadioByType(np.zeros(T, np.float32))
+    cols = np.full((T, 3), 0.5, np.float32)
+    for step, (dist, mc) in enumerate([(0.05, 5), (0.1, 3), (0.05, 5), (0.05, 2), (0.1, 3)]):
+        rec = sim.getParticleData()
+        got = sim.proximity_edges(dist, mc)
+        assert np.array_equal(got, oracle.proximity_edges(rec["pos"], rec["ptype"], dist, mc)), (step, dist, mc)
+        tris = sim.triangle_mesh(dist, mc + 1)
+        ref_tris, _ = oracle.triangle_mesh(rec["pos"], rec["ptype"], dist, mc + 1, cols, T)
+        assert np.array_equal(tris, ref_tris), (step, dist, mc)
+        sim.simulate(w.params(), 2)
+    sim.close()
