@@ -1415,7 +1415,7 @@ int proximity_enqueue(cf_world* w, float distance, int max_conn)
         CF_CUDA(launch_cell_list_csr(w->pos, w->n, g, w->ext, w->num_types, s, s.cell_off, nullptr, nullptr, w->err,
                                      &which, w->stream));
         CF_CUDA(cudaMemsetAsync(s.prox_count + w->n, 0, sizeof(uint32_t), w->stream));
-        CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.cell_off + 1, g,
+        CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.cell_off + 1, true, g,
                                         w->n, dsq, max_conn, s.prox_slots, s.prox_count, w->stream));
         CF_CUDA(launch_scan_exclusive(s.prox_count, s.prox_count, w->n + 1, s.scan_tmp, s.scan_tmp_cap, w->stream));
         CF_CUDA(cudaMemcpyAsync(&w->host_words[1], s.prox_count + w->n, sizeof(uint32_t), cudaMemcpyDeviceToHost,

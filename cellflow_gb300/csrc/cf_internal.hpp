@@ -287,10 +287,13 @@ cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const 
                                  cudaStream_t st);
 int cell_list_csr_launches(int n, const Grid& g, bool with_plan);
 int cell_list_tiles(const Grid& g);  // 0 when the rows are longer than a tile
+// csr: cell_start = CSR offsets and cell_end = offsets + 1 (rows read as
+// ranges); else per-cell start/end arrays.
 cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* keys_sorted,
                                     const uint32_t* vals_sorted, const uint32_t* cell_start,
-                                    const uint32_t* cell_end, const Grid& g, int n, float dsq, int max_conn,
-                                    int32_t* slots, uint32_t* count, cudaStream_t st);
+                                    const uint32_t* cell_end, bool csr, const Grid& g, int n, float dsq,
+                                    int max_conn, int32_t* slots, uint32_t* count, cudaStream_t st);
+// cell_start = CSR offsets, cell_end = offsets + 1.
 cudaError_t launch_mesh_select(const float4* pos_sorted, const uint32_t* keys_sorted, const uint32_t* vals_sorted,
                                const uint32_t* cell_start, const uint32_t* cell_end, const Grid& g, int n, float dsq,
                                int max_conn, int32_t* slots, uint32_t* count, cudaStream_t st);

@@ -144,8 +144,8 @@ extern "C" int cf_proximity_edges_noalloc(const void* d_pos4, int n, float width
     CF_CUDA(launch_cell_bounds(s.keys[which], s.vals[which], n, pos, s.cell_start, s.cell_end, g.cells, s.pos_sorted,
                                st));
     const float dsq = distance * distance;
-    CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_start, s.cell_end, g, n, dsq,
-                                    max_conn, s.prox_slots, s.prox_count, st));
+    CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_start, s.cell_end, false, g, n,
+                                    dsq, max_conn, s.prox_slots, s.prox_count, st));
     CF_CUDA(launch_scan_exclusive(s.prox_count, s.prox_count, n + 1, s.scan_tmp, s.scan_tmp_cap, st));
     uint32_t total = 0;
     int word = 0;

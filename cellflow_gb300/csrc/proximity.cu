@@ -21,6 +21,42 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kMaxHeld = 2 * CF_MAX_PROX_CONN;
 
+// Calls fn(u) for every sorted slot u in the cells within one cell of (cx, cy,
+// cz), clipped at the box (the proximity grid is not periodic), in cell order.
+// kCsr: cell_start = CSR offsets, cell_end = offsets + 1, so each of the
+// (at most) nine rows of the stencil is one contiguous range, read up front;
+// otherwise per-cell start/end arrays (zeros for empty cells).
+template <bool kCsr, typename Fn>
+__device__ __forceinline__ void for_each_candidate(const uint32_t* __restrict__ cell_start,
+                                                   const uint32_t* __restrict__ cell_end, const Grid& g, int cx,
+                                                   int cy, int cz, Fn fn)
+{
+    const int mx = g.m[0], my = g.m[1], mz = g.m[2];
+    const int xlo = max(cx - 1, 0), xhi = min(cx + 1, mx - 1);
+    if (kCsr) {
+        uint32_t rb[9], re[9];
+        int nr = 0;
+        for (int z = max(cz - 1, 0); z <= min(cz + 1, mz - 1); z++)
+            for (int y = max(cy - 1, 0); y <= min(cy + 1, my - 1); y++) {
+                const uint32_t row = (uint32_t)((z * my + y) * mx);
+                rb[nr] = cell_start[row + xlo];
+                re[nr] = cell_end[row + xhi];
+                nr++;
+            }
+        for (int r = 0; r < nr; r++)
+            for (uint32_t u = rb[r]; u < re[r]; u++) fn(u);
+    } else {
+        for (int z = max(cz - 1, 0); z <= min(cz + 1, mz - 1); z++)
+            for (int y = max(cy - 1, 0); y <= min(cy + 1, my - 1); y++)
+                for (int x = xlo; x <= xhi; x++) {
+                    const uint32_t cell = (uint32_t)((z * my + y) * mx + x);
+                    const uint32_t u_end = cell_end[cell];
+                    for (uint32_t u = cell_start[cell]; u < u_end; u++) fn(u);
+                }
+    }
+}
+
+template <bool kCsr>
 __global__ void __launch_bounds__(kThreads)
     proximity_select_kernel(const float4* __restrict__ pos_sorted, const uint32_t* __restrict__ keys_sorted,
                             const uint32_t* __restrict__ vals_sorted, const uint32_t* __restrict__ cell_start,
@@ -45,36 +81,28 @@ __global__ void __launch_bounds__(kThreads)
     int held = 0;
     int hj[kMaxHeld];
     float hd[kMaxHeld];
-    for (int z = max(cz - 1, 0); z <= min(cz + 1, mz - 1); z++) {
-        for (int y = max(cy - 1, 0); y <= min(cy + 1, my - 1); y++) {
-            for (int x = max(cx - 1, 0); x <= min(cx + 1, mx - 1); x++) {
-                const uint32_t cell = (uint32_t)((z * my + y) * mx + x);
-                const uint32_t u_end = cell_end[cell];
-                for (uint32_t u = cell_start[cell]; u < u_end; u++) {
-                    const float4 q = pos_sorted[u];
-                    if (__float_as_uint(q.w) != __float_as_uint(h.w)) continue;
-                    const int j = (int)vals_sorted[u];
-                    if (j <= (int)i) continue;
-                    if (held == cap && j >= hj[cap - 1]) continue;
-                    const float dx = __fsub_rn(q.x, h.x);
-                    const float dy = __fsub_rn(q.y, h.y);
-                    const float dz = __fsub_rn(q.z, h.z);
-                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                    if (!(d2 < dsq)) continue;
-                    // insert into the index-ordered set, dropping the largest when full
-                    int p = held < cap ? held : cap - 1;
-                    while (p > 0 && hj[p - 1] > j) {
-                        hj[p] = hj[p - 1];
-                        hd[p] = hd[p - 1];
-                        p--;
-                    }
-                    hj[p] = j;
-                    hd[p] = d2;
-                    if (held < cap) held++;
-                }
-            }
+    for_each_candidate<kCsr>(cell_start, cell_end, g, cx, cy, cz, [&](uint32_t u) {
+        const float4 q = pos_sorted[u];
+        if (__float_as_uint(q.w) != __float_as_uint(h.w)) return;
+        const int j = (int)vals_sorted[u];
+        if (j <= (int)i) return;
+        if (held == cap && j >= hj[cap - 1]) return;
+        const float dx = __fsub_rn(q.x, h.x);
+        const float dy = __fsub_rn(q.y, h.y);
+        const float dz = __fsub_rn(q.z, h.z);
+        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+        if (!(d2 < dsq)) return;
+        // insert into the index-ordered set, dropping the largest when full
+        int p = held < cap ? held : cap - 1;
+        while (p > 0 && hj[p - 1] > j) {
+            hj[p] = hj[p - 1];
+            hd[p] = hd[p - 1];
+            p--;
         }
-    }
+        hj[p] = j;
+        hd[p] = d2;
+        if (held < cap) held++;
+    });
     // stable insertion sort by squared distance (ParticleSimulation.cu:235-243)
     for (int a = 1; a < held; a++) {
         const float kd = hd[a];
@@ -167,32 +195,26 @@ __global__ void __launch_bounds__(kThreads)
     int held = 0;
     int hj[kMeshHeld];
     if (cap > 0) {
-        for (int z = max(cz - 1, 0); z <= min(cz + 1, mz - 1); z++)
-            for (int y = max(cy - 1, 0); y <= min(cy + 1, my - 1); y++)
-                for (int x = max(cx - 1, 0); x <= min(cx + 1, mx - 1); x++) {
-                    const uint32_t cell = (uint32_t)((z * my + y) * mx + x);
-                    const uint32_t u_end = cell_end[cell];
-                    for (uint32_t u = cell_start[cell]; u < u_end; u++) {
-                        const float4 q = pos_sorted[u];
-                        if (__float_as_uint(q.w) != __float_as_uint(h.w)) continue;
-                        const int j = (int)vals_sorted[u];
-                        if (j == (int)i) continue;
-                        if (held == cap && j >= hj[cap - 1]) continue;
-                        // ParticleSimulation.cu:314-317, rounded on its own in source order
-                        const float dx = __fsub_rn(q.x, h.x);
-                        const float dy = __fsub_rn(q.y, h.y);
-                        const float dz = __fsub_rn(q.z, h.z);
-                        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                        if (!(d2 < dsq)) continue;
-                        int p = held < cap ? held : cap - 1;
-                        while (p > 0 && hj[p - 1] > j) {
-                            hj[p] = hj[p - 1];
-                            p--;
-                        }
-                        hj[p] = j;
-                        if (held < cap) held++;
-                    }
-                }
+        for_each_candidate<true>(cell_start, cell_end, g, cx, cy, cz, [&](uint32_t u) {
+            const float4 q = pos_sorted[u];
+            if (__float_as_uint(q.w) != __float_as_uint(h.w)) return;
+            const int j = (int)vals_sorted[u];
+            if (j == (int)i) return;
+            if (held == cap && j >= hj[cap - 1]) return;
+            // ParticleSimulation.cu:314-317, rounded on its own in source order
+            const float dx = __fsub_rn(q.x, h.x);
+            const float dy = __fsub_rn(q.y, h.y);
+            const float dz = __fsub_rn(q.z, h.z);
+            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            if (!(d2 < dsq)) return;
+            int p = held < cap ? held : cap - 1;
+            while (p > 0 && hj[p - 1] > j) {
+                hj[p] = hj[p - 1];
+                p--;
+            }
+            hj[p] = j;
+            if (held < cap) held++;
+        });
     }
     // the held list is in index order: the ones above i form its tail
     int above = 0;
@@ -296,12 +318,17 @@ cudaError_t launch_mesh_emit(const int32_t* slots, const uint32_t* offsets, int 
 
 cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* keys_sorted,
                                     const uint32_t* vals_sorted, const uint32_t* cell_start,
-                                    const uint32_t* cell_end, const Grid& g, int n, float dsq, int max_conn,
-                                    int32_t* slots, uint32_t* count, cudaStream_t st)
+                                    const uint32_t* cell_end, bool csr, const Grid& g, int n, float dsq,
+                                    int max_conn, int32_t* slots, uint32_t* count, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    proximity_select_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
-        pos_sorted, keys_sorted, vals_sorted, cell_start, cell_end, g, n, dsq, max_conn, slots, count);
+    const int blocks = (n + kThreads - 1) / kThreads;
+    if (csr)
+        proximity_select_kernel<true><<<blocks, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted, cell_start,
+                                                                  cell_end, g, n, dsq, max_conn, slots, count);
+    else
+        proximity_select_kernel<false><<<blocks, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted, cell_start,
+                                                                   cell_end, g, n, dsq, max_conn, slots, count);
     return cudaGetLastError();
 }
 
