@@ -356,7 +356,7 @@ def run_gb300(args, rank, world, local):
         if world > 1:
             torch.distributed.barrier()
 
-    force_variant = sim.autotune(params, 3)  # picks the force-kernel variant; restores the state
+    force_variant = sim.autotune(params, 5)  # picks the force-kernel variant; restores the state
     for _ in range(args.warmup):
         sim.simulate(params, 1)
     sim.sync()
@@ -544,7 +544,7 @@ def run_batched(args, rank, world, local):
     batch.set_stream(stream.cuda_stream)
     batch.set_particles(pos, types)
     batch.set_force_tables(tables)
-    variant = batch.autotune(params, 3)
+    variant = batch.autotune(params, 5)
     batch.capture(params, bw.graph_steps)
     _, graph_kernels = batch.graph_info()
     replays = max(1, -(-args.steps // bw.graph_steps))
