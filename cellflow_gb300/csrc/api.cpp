@@ -116,7 +116,8 @@ void free_rollout(cf_world* w)
     for (void* p : {(void*)r.ckpt_pos, (void*)r.ckpt_vel, (void*)r.ckpt_cnt, (void*)r.seg_pos, (void*)r.seg_vel,
                     (void*)r.seg_cnt, (void*)r.fin_pos, (void*)r.fin_vel, (void*)r.fin_cnt, (void*)r.gx,
                     (void*)r.gv, (void*)r.gf_sorted, (void*)r.ga_sorted, (void*)r.gacc, (void*)r.rdf_pos,
-                    (void*)r.rdf_acc, (void*)r.type_count})
+                    (void*)r.rdf_acc, (void*)r.type_count, (void*)r.seg_sorted, (void*)r.seg_keys,
+                    (void*)r.seg_vals, (void*)r.seg_off})
         dev_free(p);
     r = Rollout();
 }
@@ -1866,6 +1867,28 @@ int ensure_rollout(cf_world* w, int ckpts, int seg_states)
     return CF_OK;
 }
 
+// Per-step cell lists of one checkpoint segment (steps = checkpoint interval).
+int ensure_rollout_lists(cf_world* w, int steps, int cells)
+{
+    Rollout& r = w->ro;
+    const size_t offs = (size_t)cells + 1;
+    if (r.seg_off && steps <= r.lists_steps && offs <= r.lists_cells) return CF_OK;
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    for (void* p : {(void*)r.seg_sorted, (void*)r.seg_keys, (void*)r.seg_vals, (void*)r.seg_off}) dev_free(p);
+    r.seg_sorted = nullptr;
+    r.seg_keys = r.seg_vals = r.seg_off = nullptr;
+    r.lists_steps = 0;
+    r.lists_cells = 0;
+    const size_t nn = (size_t)std::max(w->n, 1) * (size_t)steps;
+    CF_CUDA(dev_alloc(&r.seg_sorted, nn));
+    CF_CUDA(dev_alloc(&r.seg_keys, nn));
+    CF_CUDA(dev_alloc(&r.seg_vals, nn));
+    CF_CUDA(dev_alloc(&r.seg_off, offs * (size_t)steps));
+    r.lists_steps = steps;
+    r.lists_cells = offs;
+    return CF_OK;
+}
+
 // Radial distribution scratch (freed with the rest of the rollout buffers
 // whenever the particle count changes).
 int ensure_rdf(cf_world* w)
@@ -1902,6 +1925,10 @@ int enqueue_rollout_backward(cf_world* w, const StepConsts& c)
     CF_CUDA(cudaMemsetAsync(r.gacc, 0, sizeof(double) * kGradAccEntries, w->stream));
     const int segs = (r.steps + r.every - 1) / r.every;
     Scratch& s = w->s;
+    // keep the replay's cell lists when the tiled build is used (it always leaves the
+    // sorted keys and indices in buffer 1) and the lists are allocated for this grid
+    const bool lists = cell_list_tiles(c.grid) > 0 && r.seg_off && r.lists_steps >= std::min(r.every, r.steps) &&
+                       r.lists_cells >= (size_t)c.grid.cells + 1;
     for (int seg = segs - 1; seg >= 0; seg--) {
         const int s0 = seg * r.every;
         const int len = std::min(r.every, r.steps - s0);
@@ -1910,12 +1937,38 @@ int enqueue_rollout_backward(cf_world* w, const StepConsts& c)
         if (rc) return rc;
         for (int t = 0; t < len; t++) {
             rc = copy_state(w, r.seg_pos + n * t, r.seg_vel + n * t, r.seg_cnt + n * t, w->pos, w->vel, w->counts);
-            if (!rc) rc = enqueue_step(w, c, 0);
+            if (rc) return rc;
+            if (lists) {
+                // the replayed step builds its cell list straight into step t's arrays
+                // (the tiled build leaves it in keys[1] / vals[1]), kept for the adjoint step
+                float4* const ps = s.pos_sorted;
+                uint32_t* const k1 = s.keys[1];
+                uint32_t* const v1 = s.vals[1];
+                uint32_t* const off = s.cell_off;
+                s.pos_sorted = r.seg_sorted + n * t;
+                s.keys[1] = r.seg_keys + n * t;
+                s.vals[1] = r.seg_vals + n * t;
+                s.cell_off = r.seg_off + r.lists_cells * t;
+                rc = enqueue_step(w, c, 0);
+                s.pos_sorted = ps;
+                s.keys[1] = k1;
+                s.vals[1] = v1;
+                s.cell_off = off;
+            } else {
+                rc = enqueue_step(w, c, 0);
+            }
             if (rc) return rc;
         }
         CF_CUDA(cudaMemcpyAsync(r.seg_cnt + n * len, w->counts, sizeof(int) * n, cudaMemcpyDeviceToDevice,
                                 w->stream));
         for (int t = len - 1; t >= 0; t--) {
+            if (lists) {
+                CF_CUDA(launch_adjoint_step(c, w->tables, r.seg_sorted + n * t, r.seg_keys + n * t,
+                                            r.seg_vals + n * t, r.seg_off + r.lists_cells * t, r.seg_vel + n * t,
+                                            r.seg_cnt + n * t, r.seg_cnt + n * (t + 1), r.gx, r.gv, r.gf_sorted,
+                                            r.ga_sorted, r.gacc, w->stream));
+                continue;
+            }
             int which = 0;
             CF_CUDA(launch_cell_list_csr(r.seg_pos + n * t, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, nullptr,
                                          nullptr, w->err, &which, w->stream));
@@ -2000,6 +2053,7 @@ int cf_rollout_backward(cf_world* w, const float* d_gpos4, const float* d_gvel4,
     if (!rc) rc = ensure_cells(w, c.grid.cells);
     if (!rc) rc = ensure_plan(w, c.grid);
     if (!rc) rc = ensure_offsets(w, c.grid.cells);
+    if (!rc) rc = ensure_rollout_lists(w, std::min(r.every, r.steps), c.grid.cells);
     if (rc) return rc;
     const size_t n = (size_t)w->n;
     if (d_gpos4)
@@ -2013,7 +2067,7 @@ int cf_rollout_backward(cf_world* w, const float* d_gpos4, const float* d_gvel4,
     if (w->use_graphs && w->stream != nullptr) {
         const void* bufs = w->s.cell_start;
         const bool same = r.bwd_graph && r.bwd_steps == r.steps && r.bwd_every == r.every && r.bwd_bufs == bufs &&
-                          std::memcmp(&r.bwd_key, &c, sizeof(c)) == 0;
+                          r.bwd_lists == r.seg_off && std::memcmp(&r.bwd_key, &c, sizeof(c)) == 0;
         if (!same) {
             if (r.bwd_graph) cudaGraphExecDestroy(r.bwd_graph);
             r.bwd_graph = nullptr;
@@ -2033,6 +2087,7 @@ int cf_rollout_backward(cf_world* w, const float* d_gpos4, const float* d_gvel4,
             r.bwd_steps = r.steps;
             r.bwd_every = r.every;
             r.bwd_bufs = bufs;
+            r.bwd_lists = r.seg_off;
         }
         CF_CUDA(cudaGraphLaunch(r.bwd_graph, w->stream));
     } else {

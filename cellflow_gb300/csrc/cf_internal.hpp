@@ -150,6 +150,14 @@ struct Rollout {
     float4* fin_pos = nullptr;  // the state after the forward, restored after the backward
     float4* fin_vel = nullptr;
     int* fin_cnt = nullptr;
+    // the cell list of every replayed step of a segment (sorted snapshot, sorted
+    // keys and indices, CSR offsets), written by the replay, read by the adjoint step
+    float4* seg_sorted = nullptr;
+    uint32_t* seg_keys = nullptr;
+    uint32_t* seg_vals = nullptr;
+    uint32_t* seg_off = nullptr;
+    int lists_steps = 0;   // steps the lists hold
+    size_t lists_cells = 0;  // cells + 1 per step's offsets
     float4* gx = nullptr;         // dL/dx of the current step boundary
     float4* gv = nullptr;         // dL/dv
     float4* gf_sorted = nullptr;  // dL/df per particle, cell order
@@ -167,6 +175,7 @@ struct Rollout {
     StepConsts bwd_key{};
     int bwd_steps = 0, bwd_every = 0;
     const void* bwd_bufs = nullptr;
+    const void* bwd_lists = nullptr;
     // radial distribution scratch
     float4* rdf_pos = nullptr;
     double* rdf_acc = nullptr;
