@@ -143,13 +143,21 @@ __global__ void __launch_bounds__(kAdjThreads)
 {
     __shared__ float s_gF[kTableSize];
     __shared__ float s_par[8];
-    for (int q = threadIdx.x; q < kTableSize; q += blockDim.x) s_gF[q] = 0.0f;
+    __shared__ float s_thr[kTableSize], s_inv_eff[kTableSize], s_F[kTableSize];
+    for (int q = threadIdx.x; q < kTableSize; q += blockDim.x) {
+        s_gF[q] = 0.0f;
+        s_thr[q] = tables->threshold[q];
+        s_inv_eff[q] = tables->eff[q] > 0.0f ? 1.0f / tables->eff[q] : 0.0f;
+        s_F[q] = tables->force[q];
+    }
     if (threadIdx.x < 8) s_par[threadIdx.x] = 0.0f;
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
+    const float c2 = -c.neg_k;  // k
+    const float c2_log2 = c.neg_k * 1.4426950408889634f;  // -k log2(e): e = 2^(c2_log2 r^2)
     const int warps = (int)(gridDim.x * (blockDim.x >> 5));
-    const float R = c.repulsion, A = c.attraction, kk = -c.neg_k;
+    const float R = c.repulsion, A = c.attraction;
     const int m0 = c.grid.m[0], m1 = c.grid.m[1], m2 = c.grid.m[2];
     int ylo, yhi, zlo, zhi;
     axis_range(m1, ylo, yhi);
@@ -185,17 +193,20 @@ __global__ void __launch_bounds__(kAdjThreads)
                         const float s = __fadd_rn(d2, 0.0001f);
                         const uint32_t tj = type_of(o);
                         const int pair = ti * kTableStride + tj;
-                        if (!(s < tables->threshold[pair])) continue;
-                        const float eff = tables->eff[pair];
-                        const float dist = sqrtf(s);
-                        const float r = dist / eff;
-                        const float e = expf(-kk * r * r);
+                        if (!(s < s_thr[pair])) continue;
+                        // rsqrt and exp2 approximations (a few ulp): the gradient's tolerance
+                        // is far wider than the forward's
+                        const float inv_eff = s_inv_eff[pair];
+                        const float inv_d = rsqrtf(s);
+                        const float dist = s * inv_d;
+                        const float r = dist * inv_eff;
+                        float e;
+                        asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(c2_log2 * r * r));
                         const float nraw = R * e - A * r;
-                        const float dn = (R * e * (-2.0f * kk * r) - A) / eff;
-                        const float inv_d = 1.0f / dist;
+                        const float dn = (R * e * (-2.0f * c2 * r) - A) * inv_eff;
                         const float phi = nraw * inv_d;
                         const float hc = (dn * dist - nraw) * inv_d * inv_d * inv_d;
-                        const float Fij = tables->force[pair], Fji = tables->force[tj * kTableStride + ti];
+                        const float Fij = s_F[pair], Fji = s_F[tj * kTableStride + ti];
                         const float4 gfj = gf_sorted[q];
                         const float wx = Fji * gfj.x - Fij * gfi.x, wy = Fji * gfj.y - Fij * gfi.y,
                                     wz = Fji * gfj.z - Fij * gfi.z;
