@@ -478,8 +478,8 @@ cudaError_t launch_adjoint_step(const StepConsts& c, const PairTables* tables, c
     const int blocks = (c.n + kAdjThreads - 1) / kAdjThreads;
     adj_prep_kernel<<<blocks, kAdjThreads, 0, st>>>(c, vals_sorted, vel, cnt_prev, cnt_new, gx, gv, gf_sorted,
                                                      ga_sorted, gacc);
-    // one warp per home, grid-stride: four blocks of four warps per SM
-    const int pair_blocks = std::min((c.n + kAdjThreads / 32 - 1) / (kAdjThreads / 32), 4 * num_sms());
+    // one warp per home, grid-stride: eight blocks of four warps per SM
+    const int pair_blocks = std::min((c.n + kAdjThreads / 32 - 1) / (kAdjThreads / 32), 8 * num_sms());
     adj_pair_kernel<<<pair_blocks, kAdjThreads, 0, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off,
                                                           gf_sorted, ga_sorted, gx, gacc);
     return cudaGetLastError();
