@@ -300,26 +300,31 @@ __device__ __forceinline__ float bspline3_d(float t)
     return t < 0.0f ? -g : g;
 }
 
-// Calls fn(q, o, dx, dy, dz, r) for every other particle q (position o) within r_cut of home k.
+// Calls fn(q, o, dx, dy, dz, r) for every other particle q (position o) within r_cut of
+// home k. A warp shares the walk: its lanes stride over each stencil row's particles (at
+// most two runs of consecutive cells per row, contiguous ranges of the sorted snapshot).
 template <typename Fn>
-__device__ __forceinline__ void rdf_neighbours(const RdfConsts& c, const float4* __restrict__ pos_sorted,
-                                               const uint32_t* __restrict__ keys,
-                                               const uint32_t* __restrict__ cell_off, int k, const float4& h, Fn fn)
+__device__ __forceinline__ void rdf_neighbours_warp(const RdfConsts& c, const float4* __restrict__ pos_sorted,
+                                                    const uint32_t* __restrict__ keys,
+                                                    const uint32_t* __restrict__ cell_off, int k, const float4& h,
+                                                    int lane, Fn fn)
 {
     const int m0 = c.m[0], m1 = c.m[1], m2 = c.m[2];
     const uint32_t cell = keys[k];
     const int cx = (int)(cell % (uint32_t)m0), cy = (int)((cell / (uint32_t)m0) % (uint32_t)m1),
               cz = (int)(cell / ((uint32_t)m0 * (uint32_t)m1));
-    int xlo, xhi, ylo, yhi, zlo, zhi;
-    axis_range(m0, xlo, xhi);
+    int ylo, yhi, zlo, zhi, a0, b0, a1, b1;
     axis_range(m1, ylo, yhi);
     axis_range(m2, zlo, zhi);
+    x_runs(cx, m0, a0, b0, a1, b1);
     for (int oz = zlo; oz <= zhi; oz++)
-        for (int oy = ylo; oy <= yhi; oy++)
-            for (int ox = xlo; ox <= xhi; ox++) {
-                const int c2 = (wrap_cell(cz + oz, m2) * m1 + wrap_cell(cy + oy, m1)) * m0 + wrap_cell(cx + ox, m0);
-                const uint32_t qb = cell_off[c2], qe = cell_off[c2 + 1];
-                for (uint32_t q = qb; q < qe; q++) {
+        for (int oy = ylo; oy <= yhi; oy++) {
+            const int row = (wrap_cell(cz + oz, m2) * m1 + wrap_cell(cy + oy, m1)) * m0;
+            for (int run = 0; run < 2; run++) {
+                const int ra = run ? a1 : a0, rb = run ? b1 : b0;
+                if (rb < ra) continue;
+                const uint32_t qb = cell_off[row + ra], qe = cell_off[row + rb + 1];
+                for (uint32_t q = qb + lane; q < qe; q += 32) {
                     if ((int)q == k) continue;
                     const float4 o = pos_sorted[q];
                     const float dx = wrap_ref(o.x - h.x, c.ext[0], c.half[0]);
@@ -329,8 +334,10 @@ __device__ __forceinline__ void rdf_neighbours(const RdfConsts& c, const float4*
                     if (r < c.r_cut) fn(q, o, dx, dy, dz, r);
                 }
             }
+        }
 }
 
+// One warp per home (grid-stride), the histogram in shared memory per block.
 __global__ void rdf_kernel(RdfConsts c, const float4* __restrict__ pos_sorted, const uint32_t* __restrict__ keys,
                            const uint32_t* __restrict__ cell_off, double* __restrict__ acc,
                            unsigned long long* __restrict__ type_count)
@@ -341,21 +348,23 @@ __global__ void rdf_kernel(RdfConsts c, const float4* __restrict__ pos_sorted, c
     for (int q = threadIdx.x; q < H; q += blockDim.x) s_hist[q] = 0.0f;
     if (threadIdx.x < CF_MAX_TYPES) s_count[threadIdx.x] = 0u;
     __syncthreads();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    // a type outside [0, T) is reported by the cell list's hash; skip it here
-    if (k < c.n && type_of(pos_sorted[k]) < (uint32_t)c.T) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (int)(gridDim.x * (blockDim.x >> 5));
+    for (int k = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); k < c.n; k += warps) {
         const float4 h = pos_sorted[k];
         const uint32_t ti = type_of(h);
-        atomicAdd(&s_count[ti], 1u);
-        rdf_neighbours(c, pos_sorted, keys, cell_off, k, h,
-                       [&](uint32_t, const float4& o, float, float, float, float r) {
-                           if (type_of(o) >= (uint32_t)c.T) return;
-                           const float t0 = r * c.inv_bin - 0.5f;
-                           const int k0 = max(0, (int)ceilf(t0 - 2.0f));
-                           const int k1 = min(c.bins - 1, (int)floorf(t0 + 2.0f));
-                           float* row = s_hist + ((int)ti * c.T + (int)type_of(o)) * c.bins;
-                           for (int b = k0; b <= k1; b++) atomicAdd(&row[b], bspline3(t0 - (float)b));
-                       });
+        // a type outside [0, T) is reported by the cell list's hash; skip it here
+        if (ti >= (uint32_t)c.T) continue;
+        if (lane == 0) atomicAdd(&s_count[ti], 1u);
+        rdf_neighbours_warp(c, pos_sorted, keys, cell_off, k, h, lane,
+                            [&](uint32_t, const float4& o, float, float, float, float r) {
+                                if (type_of(o) >= (uint32_t)c.T) return;
+                                const float t0 = r * c.inv_bin - 0.5f;
+                                const int k0 = max(0, (int)ceilf(t0 - 2.0f));
+                                const int k1 = min(c.bins - 1, (int)floorf(t0 + 2.0f));
+                                float* row = s_hist + ((int)ti * c.T + (int)type_of(o)) * c.bins;
+                                for (int b = k0; b <= k1; b++) atomicAdd(&row[b], bspline3(t0 - (float)b));
+                            });
     }
     __syncthreads();
     for (int q = threadIdx.x; q < H; q += blockDim.x)
@@ -404,30 +413,35 @@ __global__ void rdf_grad_kernel(RdfConsts c, const float4* __restrict__ pos_sort
         s_g[q] = den > 0.0 ? (float)((double)ghist[q] / den) : 0.0f;
     }
     __syncthreads();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= c.n) return;
-    const float4 h = pos_sorted[k];
-    const uint32_t ti = type_of(h);
-    float ax = 0.0f, ay = 0.0f, az = 0.0f;
-    // a type outside [0, T) is reported by the cell list's hash; it contributes nothing here
-    if (ti < (uint32_t)c.T)
-        rdf_neighbours(c, pos_sorted, keys, cell_off, k, h,
-                   [&](uint32_t, const float4& o, float dx, float dy, float dz, float r) {
-                       const uint32_t tj = type_of(o);
-                       if (!(r > 0.0f) || tj >= (uint32_t)c.T) return;
-                       const float t0 = r * c.inv_bin - 0.5f;
-                       const int k0 = max(0, (int)ceilf(t0 - 2.0f));
-                       const int k1 = min(c.bins - 1, (int)floorf(t0 + 2.0f));
-                       const float* gij = s_g + ((int)ti * c.T + (int)tj) * c.bins;
-                       const float* gji = s_g + ((int)tj * c.T + (int)ti) * c.bins;
-                       float G = 0.0f;
-                       for (int b = k0; b <= k1; b++) G += (gij[b] + gji[b]) * bspline3_d(t0 - (float)b);
-                       const float s = G * c.inv_bin / r;
-                       ax -= s * dx;
-                       ay -= s * dy;
-                       az -= s * dz;
-                   });
-    gpos[vals[k]] = make_float4(ax, ay, az, 0.0f);
+    const int lane = threadIdx.x & 31;
+    const int warps = (int)(gridDim.x * (blockDim.x >> 5));
+    for (int k = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); k < c.n; k += warps) {
+        const float4 h = pos_sorted[k];
+        const uint32_t ti = type_of(h);
+        float ax = 0.0f, ay = 0.0f, az = 0.0f;
+        // a type outside [0, T) is reported by the cell list's hash; it contributes nothing here
+        if (ti < (uint32_t)c.T)
+            rdf_neighbours_warp(c, pos_sorted, keys, cell_off, k, h, lane,
+                                [&](uint32_t, const float4& o, float dx, float dy, float dz, float r) {
+                                    const uint32_t tj = type_of(o);
+                                    if (!(r > 0.0f) || tj >= (uint32_t)c.T) return;
+                                    const float t0 = r * c.inv_bin - 0.5f;
+                                    const int k0 = max(0, (int)ceilf(t0 - 2.0f));
+                                    const int k1 = min(c.bins - 1, (int)floorf(t0 + 2.0f));
+                                    const float* gij = s_g + ((int)ti * c.T + (int)tj) * c.bins;
+                                    const float* gji = s_g + ((int)tj * c.T + (int)ti) * c.bins;
+                                    float G = 0.0f;
+                                    for (int b = k0; b <= k1; b++) G += (gij[b] + gji[b]) * bspline3_d(t0 - (float)b);
+                                    const float s = G * c.inv_bin / r;
+                                    ax -= s * dx;
+                                    ay -= s * dy;
+                                    az -= s * dz;
+                                });
+        ax = warp_sum(ax);
+        ay = warp_sum(ay);
+        az = warp_sum(az);
+        if (lane == 0) gpos[vals[k]] = make_float4(ax, ay, az, 0.0f);
+    }
 }
 
 // dst.xyz = src.xyz, dst.w = typesrc.w (the particle's type bits).
@@ -501,9 +515,11 @@ cudaError_t launch_rdf(const float* ext, const Grid& g, int n, int T, int bins, 
     cudaError_t e = cudaMemsetAsync(acc, 0, sizeof(double) * H, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(type_count, 0, sizeof(unsigned long long) * CF_MAX_TYPES, st);
     if (e != cudaSuccess) return e;
+    // one warp per home, grid-stride; two blocks per SM keep the histogram flushes few
+    const int warps_per_block = kAdjThreads / 32;
     if (n > 0)
-        rdf_kernel<<<(n + kAdjThreads - 1) / kAdjThreads, kAdjThreads, rdf_smem_bytes(T, bins), st>>>(
-            c, pos_sorted, keys_sorted, cell_off, acc, type_count);
+        rdf_kernel<<<std::min((n + warps_per_block - 1) / warps_per_block, 2 * num_sms()), kAdjThreads,
+                     rdf_smem_bytes(T, bins), st>>>(c, pos_sorted, keys_sorted, cell_off, acc, type_count);
     rdf_finish_kernel<<<(H + 255) / 256, 256, 0, st>>>(c, acc, type_count, hist);
     return cudaGetLastError();
 }
@@ -517,8 +533,10 @@ cudaError_t launch_rdf_grad(const float* ext, const Grid& g, int n, int T, int b
     cudaError_t e = cudaMemsetAsync(type_count, 0, sizeof(unsigned long long) * CF_MAX_TYPES, st);
     if (e != cudaSuccess || n == 0) return e;
     type_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, n, type_count);
-    rdf_grad_kernel<<<(n + kAdjThreads - 1) / kAdjThreads, kAdjThreads, rdf_smem_bytes(T, bins), st>>>(
-        c, pos_sorted, keys_sorted, vals_sorted, cell_off, ghist, type_count, gpos);
+    const int warps_per_block = kAdjThreads / 32;
+    rdf_grad_kernel<<<std::min((n + warps_per_block - 1) / warps_per_block, 8 * num_sms()), kAdjThreads,
+                      rdf_smem_bytes(T, bins), st>>>(c, pos_sorted, keys_sorted, vals_sorted, cell_off, ghist,
+                                                     type_count, gpos);
     return cudaGetLastError();
 }
 
