@@ -368,6 +368,7 @@ def run_gb300(args, rank, world, local):
                           if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else local)
     clocks.start()
     barrier()
+    tally0 = lib.cf_kernel_launches()
     wall0 = time.perf_counter()
     with torch.cuda.stream(stream):
         for _ in range(args.steps):
@@ -375,6 +376,7 @@ def run_gb300(args, rank, world, local):
             sim.simulate(params, 1)
     barrier()
     wall = time.perf_counter() - wall0
+    launches = lib.cf_kernel_launches() - tally0
     clk = clocks.stop()
     prof = _lib.PhaseTimes()
     _lib.check(lib.cf_profile_read(sim.handle, C.byref(prof)), "cf_profile_read")
@@ -492,7 +494,8 @@ def run_gb300(args, rank, world, local):
                     "path": "cf_step_host: pinned 44-B AoS records up, one step, records back (one CUDA graph)",
                     "three_calls": {"value": w.n * e2e_steps * world / e2e_three_wall, "unit": "particle-steps/s",
                                     "path": "cf_set_particles + cf_step + cf_get_particles"}},
-            "gpu_launches": int(prof.launches),
+            "gpu_launches": int(launches),
+            "gpu_launches_expected": int(prof.launches),
             "clocks": clk,
             "wall_s_timed_region": wall,
             "cpu_baseline": cpu,
@@ -557,6 +560,7 @@ def run_batched(args, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
+    tally0 = _lib.load().cf_kernel_launches()
     with torch.cuda.stream(stream):
         for e0, e1 in ev:
             flush.zero_()
@@ -564,6 +568,7 @@ def run_batched(args, rank, world, local):
             batch.replay()
             e1.record(stream)
     barrier()
+    launches = _lib.load().cf_kernel_launches() - tally0
     clk = clocks.stop()
     batch_ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
     t_max = max_over_ranks(batch_ms)
@@ -639,7 +644,7 @@ def run_batched(args, rank, world, local):
                     bw.graph_steps, "d2h_bytes_per_step": total * 36 // bw.graph_steps,
                     "path": "cf_batch_set_state (pinned) + 100-step graph replay + cf_batch_get_state",
                     "replays": e2e_reps},
-            "gpu_launches": graph_kernels * replays,
+            "gpu_launches": int(launches), "gpu_launches_expected": graph_kernels * replays,
             "clocks": clk,
             "library": cf.__name__ + ": " + lib.cf_version().decode(),
         }
@@ -728,7 +733,9 @@ def run_rollout(args, rank, world, local):
     fwd_plain = timed(lambda: sim.simulate(params, K), reps)
     fwd_roll = timed(lambda: sim.rollout_forward(params, K, cfg["every"], None, None, None, None), reps)
     bwd = timed(lambda: sim.rollout_backward(gx.data_ptr(), None, g0.data_ptr(), gv0.data_ptr()), reps)
+    tally0 = lib.cf_kernel_launches()
     train = timed(train_step, reps)
+    launches = lib.cf_kernel_launches() - tally0
     clk = clocks.stop()
     med = statistics.median
     step_fwd = med(fwd_plain) / K
@@ -767,7 +774,7 @@ def run_rollout(args, rank, world, local):
             "e2e": {"value": n * K / med(e2e), "unit": "particle-steps/s", "h2d_bytes_per_step": n * 16,
                     "d2h_bytes_per_step": n * 16 + 4 * (T * T + 6),
                     "path": "pinned positions in, rollout + loss + adjoint, pinned position gradients out"},
-            "gpu_launches": None, "clocks": clk,
+            "gpu_launches": int(launches), "clocks": clk,
             "library": cf.__name__ + ": " + lib.cf_version().decode(),
         }
         print(json.dumps(line), flush=True)
@@ -897,12 +904,18 @@ def reference_gpu_kernel(w, params, pos, types, table, radio, stream):
 
 def profile_steps(args) -> None:
     """--profile-steps S: S plain steps of the workload from its initial state under one force-kernel
-    variant, nothing timed, for an ncu capture of step k with `-k regex:step_force_kernel -s k-1 -c 1`."""
+    variant, nothing timed, for an ncu capture of step k with `-k regex:step_force_kernel -s k-1 -c 1`;
+    then, where the workload has a proximity distance, one proximity-graph call (device vertices,
+    the reference's call shape).  For a rollout workload: one forward + loss + backward pass of an
+    S-step rollout instead (zero loss target), the launch sequence of one training pass."""
     import numpy as np
 
     from cellflow_gb300 import inputs
     from cellflow_gb300.world import ParticleSimulation
 
+    if args.workload in ROLLOUT:
+        profile_rollout(args)
+        return
     w = inputs.WORKLOADS[args.workload]
     params = w.params()
     sim = ParticleSimulation(w.n, w.num_types, w.extent, w.extent, w.extent)
@@ -913,8 +926,53 @@ def profile_steps(args) -> None:
         sim.set_force_variant(args.variant)
     sim.simulate(params, args.profile_steps)
     sim.sync()
+    edges = None
+    if w.prox_distance is not None:
+        import torch
+
+        cap_v = 2 * w.n * w.prox_max_conn
+        verts = torch.empty(cap_v * 6, dtype=torch.float32, device="cuda")
+        colors = [(1.0, 1.0, 1.0)] * w.num_types
+        edges = sim.proximity_vertices_device(w.prox_distance, w.prox_max_conn, colors, verts.data_ptr(), cap_v) // 2
     sim.close()
-    print(json.dumps({"profile_steps": args.profile_steps, "workload": w.name, "variant": args.variant}))
+    print(json.dumps({"profile_steps": args.profile_steps, "workload": w.name, "variant": args.variant,
+                      "proximity_edges": edges}))
+
+
+def profile_rollout(args) -> None:
+    """--profile-steps S on a rollout workload: one S-step training pass (cf_rollout_forward,
+    cf_rdf, cf_rdf_backward, cf_rollout_backward) on the workload's world, nothing timed."""
+    import numpy as np
+    import torch
+
+    from cellflow_gb300 import inputs
+    from cellflow_gb300.world import ParticleSimulation
+
+    cfg = ROLLOUT[args.workload]
+    n, T, K = cfg["n"], cfg["types"], args.profile_steps
+    w = inputs.Workload(args.workload, n=n, num_types=T, radius=cfg["radius"], steps=K, seed=cfg["seed"])
+    params = w.params()
+    stream = torch.cuda.Stream()
+    sim = ParticleSimulation(n, T, w.extent, w.extent, w.extent)
+    sim.set_stream(stream.cuda_stream)
+    sim.set_particles(w.positions(), w.types())
+    sim.setForceTable(w.table())
+    sim.setRadioByType(np.zeros(T, np.float32))
+    bins, r_max = cfg["bins"], cfg["r_max"]
+    with torch.cuda.stream(stream):
+        hist = torch.empty((T, T, bins), dtype=torch.float32, device="cuda")
+        ghist = torch.empty_like(hist)
+        xk, gx, g0, gv0 = (torch.empty((n, 4), dtype=torch.float32, device="cuda") for _ in range(4))
+    stream.synchronize()
+    sim.rollout_forward(params, K, min(cfg["every"], K), None, None, xk.data_ptr(), None)
+    sim.rdf(bins, r_max, hist.data_ptr(), xk.data_ptr())
+    with torch.cuda.stream(stream):
+        torch.mul(hist, 2.0 / hist.numel(), out=ghist)
+    sim.rdf_backward(bins, r_max, ghist.data_ptr(), gx.data_ptr(), xk.data_ptr())
+    sim.rollout_backward(gx.data_ptr(), None, g0.data_ptr(), gv0.data_ptr())
+    sim.sync()
+    sim.close()
+    print(json.dumps({"profile_steps": K, "workload": args.workload}))
 
 
 def main():

@@ -144,6 +144,7 @@ _P = C.POINTER
 _SIGNATURES = {
     "cf_last_error": (C.c_char_p, []),
     "cf_version": (C.c_char_p, []),
+    "cf_kernel_launches": (C.c_longlong, []),
     "cf_default_params": (None, [_P(StepParams)]),
     "cf_create": (C.c_int, [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_uint64, _P(_W)]),
     "cf_destroy": (C.c_int, [_W]),

@@ -492,10 +492,12 @@ cudaError_t launch_adjoint_step(const StepConsts& c, const PairTables* tables, c
     const int blocks = (c.n + kAdjThreads - 1) / kAdjThreads;
     adj_prep_kernel<<<blocks, kAdjThreads, 0, st>>>(c, vals_sorted, vel, cnt_prev, cnt_new, gx, gv, gf_sorted,
                                                      ga_sorted, gacc);
+    note_launches(st);
     // one warp per home, grid-stride: eight blocks of four warps per SM
     const int pair_blocks = std::min((c.n + kAdjThreads / 32 - 1) / (kAdjThreads / 32), 8 * num_sms());
     adj_pair_kernel<<<pair_blocks, kAdjThreads, 0, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off,
                                                           gf_sorted, ga_sorted, gx, gacc);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -503,6 +505,7 @@ cudaError_t launch_pack_pos(const float4* src, const float4* typesrc, float4* ds
 {
     if (n == 0) return cudaSuccess;
     pack_pos_kernel<<<(n + 255) / 256, 256, 0, st>>>(src, typesrc, dst, n);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -517,10 +520,13 @@ cudaError_t launch_rdf(const float* ext, const Grid& g, int n, int T, int bins, 
     if (e != cudaSuccess) return e;
     // one warp per home, grid-stride; two blocks per SM keep the histogram flushes few
     const int warps_per_block = kAdjThreads / 32;
-    if (n > 0)
+    if (n > 0) {
         rdf_kernel<<<std::min((n + warps_per_block - 1) / warps_per_block, 2 * num_sms()), kAdjThreads,
                      rdf_smem_bytes(T, bins), st>>>(c, pos_sorted, keys_sorted, cell_off, acc, type_count);
+        note_launches(st);
+    }
     rdf_finish_kernel<<<(H + 255) / 256, 256, 0, st>>>(c, acc, type_count, hist);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -533,10 +539,12 @@ cudaError_t launch_rdf_grad(const float* ext, const Grid& g, int n, int T, int b
     cudaError_t e = cudaMemsetAsync(type_count, 0, sizeof(unsigned long long) * CF_MAX_TYPES, st);
     if (e != cudaSuccess || n == 0) return e;
     type_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(pos, n, type_count);
+    note_launches(st);
     const int warps_per_block = kAdjThreads / 32;
     rdf_grad_kernel<<<std::min((n + warps_per_block - 1) / warps_per_block, 8 * num_sms()), kAdjThreads,
                       rdf_smem_bytes(T, bins), st>>>(c, pos_sorted, keys_sorted, vals_sorted, cell_off, ghist,
                                                      type_count, gpos);
+    note_launches(st);
     return cudaGetLastError();
 }
 

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -498,7 +499,8 @@ int step_graph(cf_world* w, const StepConsts& c, int prof, cudaGraphExec_t* out)
         return rc;
     }
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&w->graph[prof], graph, 0);
+    e = graph_kernel_count(graph, &w->graph_kernels[prof]);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&w->graph[prof], graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
     w->graph_key[prof] = c;
@@ -549,6 +551,36 @@ int cuda_fail(cudaError_t e, const char* what)
 {
     g_error = std::string(what) + ": " + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? CF_ERR_ALLOC : CF_ERR_CUDA;
+}
+
+namespace {
+std::atomic<long long> g_launches{0};
+}
+
+void note_launches(cudaStream_t st, long long k)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    // a launch recorded into a graph is counted when the graph is launched
+    if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) return;
+    g_launches.fetch_add(k, std::memory_order_relaxed);
+}
+
+long long launch_tally() { return g_launches.load(std::memory_order_relaxed); }
+
+cudaError_t graph_kernel_count(cudaGraph_t graph, long long* kernels)
+{
+    *kernels = 0;
+    size_t nodes = 0;
+    cudaError_t e = cudaGraphGetNodes(graph, nullptr, &nodes);
+    if (e != cudaSuccess || nodes == 0) return e;
+    std::vector<cudaGraphNode_t> list(nodes);
+    e = cudaGraphGetNodes(graph, list.data(), &nodes);
+    for (size_t i = 0; i < nodes && e == cudaSuccess; i++) {
+        cudaGraphNodeType t;
+        e = cudaGraphNodeGetType(list[i], &t);
+        if (e == cudaSuccess && t == cudaGraphNodeTypeKernel) ++*kernels;
+    }
+    return e;
 }
 
 // Smallest float t >= 0 with sqrtf(t) >= eff.  sqrtf is monotone, so for
@@ -676,6 +708,8 @@ extern "C" {
 const char* cf_last_error(void) { return g_error.c_str(); }
 
 const char* cf_version(void) { return "cellflow-gb300 0.1 (sm_103a)"; }
+
+long long cf_kernel_launches(void) { return launch_tally(); }
 
 void cf_default_params(cf_step_params* p)
 {
@@ -1044,9 +1078,10 @@ int cf_step(cf_world* w, const cf_step_params* p, int nsteps)
     }
     const long long launches = cell_list_csr_launches(w->n, c.grid, true) + step_launches(w->n);
     for (int s = 0; s < nsteps; s++) {
-        if (exec)
+        if (exec) {
             CF_CUDA(cudaGraphLaunch(exec, w->stream));
-        else {
+            note_launches(w->stream, w->graph_kernels[prof]);
+        } else {
             rc = enqueue_step(w, c, prof);
             if (rc) return rc;
         }
@@ -1133,7 +1168,8 @@ int cf_step_host(cf_world* w, const cf_step_params* p, const cf_particle* in, cf
             return rc;
         }
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&w->host_graph, graph, 0);
+        e = graph_kernel_count(graph, &w->host_graph_kernels);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&w->host_graph, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
         w->host_key = c;
@@ -1142,6 +1178,7 @@ int cf_step_host(cf_world* w, const cf_step_params* p, const cf_particle* in, cf
         w->host_bufs = bufs;
     }
     CF_CUDA(cudaGraphLaunch(w->host_graph, w->stream));
+    note_launches(w->stream, w->host_graph_kernels);
     CF_CUDA(cudaStreamSynchronize(w->stream));
     const int word = w->host_words[0];
     if (word) {
@@ -1384,7 +1421,8 @@ int run_selection(cf_world* w, int kind, const Grid& g, float dsq, int max_conn,
             return rc;
         }
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&sg.exec, graph, 0);
+        e = graph_kernel_count(graph, &sg.kernels);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&sg.exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
         sg.g = g;
@@ -1394,6 +1432,7 @@ int run_selection(cf_world* w, int kind, const Grid& g, float dsq, int max_conn,
         sg.types = w->num_types;
     }
     CF_CUDA(cudaGraphLaunch(sg.exec, w->stream));
+    note_launches(w->stream, sg.kernels);
     return CF_OK;
 }
 }  // extern "C++"
@@ -1765,18 +1804,8 @@ int cf_batch_capture(cf_batch* b, const cf_step_params* p, int nsteps)
         return rc;
     }
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-    size_t nodes = 0;
     long long kernels = 0;
-    e = cudaGraphGetNodes(graph, nullptr, &nodes);
-    if (e == cudaSuccess && nodes) {
-        std::vector<cudaGraphNode_t> list(nodes);
-        e = cudaGraphGetNodes(graph, list.data(), &nodes);
-        for (size_t i = 0; i < nodes && e == cudaSuccess; i++) {
-            cudaGraphNodeType t;
-            e = cudaGraphNodeGetType(list[i], &t);
-            if (e == cudaSuccess && t == cudaGraphNodeTypeKernel) kernels++;
-        }
-    }
+    e = graph_kernel_count(graph, &kernels);
     if (e != cudaSuccess) {
         cudaGraphDestroy(graph);
         return cuda_fail(e, "cudaGraphGetNodes");
@@ -1804,6 +1833,7 @@ int cf_batch_replay(cf_batch* b)
     if (rc) return rc;
     if (!b->w->batch_graph) return fail(CF_ERR_INVALID, "no captured graph (cf_batch_capture)");
     CF_CUDA(cudaGraphLaunch(b->w->batch_graph, b->w->stream));
+    note_launches(b->w->stream, b->w->batch_graph_kernels);
     return CF_OK;
 }
 
@@ -2019,10 +2049,12 @@ int cf_rollout_forward(cf_world* w, const cf_step_params* p, const float* d_pos4
             rc = copy_state(w, r.ckpt_pos + n * k, r.ckpt_vel + n * k, r.ckpt_cnt + n * k, w->pos, w->vel, w->counts);
             if (rc) return rc;
         }
-        if (exec)
+        if (exec) {
             CF_CUDA(cudaGraphLaunch(exec, w->stream));
-        else if ((rc = enqueue_step(w, c, 0)))
+            note_launches(w->stream, w->graph_kernels[0]);
+        } else if ((rc = enqueue_step(w, c, 0))) {
             return rc;
+        }
     }
     if (d_pos4_out)
         CF_CUDA(cudaMemcpyAsync(d_pos4_out, w->pos, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
@@ -2080,7 +2112,8 @@ int cf_rollout_backward(cf_world* w, const float* d_gpos4, const float* d_gvel4,
                 return rc;
             }
             if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-            e = cudaGraphInstantiate(&r.bwd_graph, graph, 0);
+            e = graph_kernel_count(graph, &r.bwd_kernels);
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&r.bwd_graph, graph, 0);
             cudaGraphDestroy(graph);
             if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
             r.bwd_key = c;
@@ -2090,6 +2123,7 @@ int cf_rollout_backward(cf_world* w, const float* d_gpos4, const float* d_gvel4,
             r.bwd_lists = r.seg_off;
         }
         CF_CUDA(cudaGraphLaunch(r.bwd_graph, w->stream));
+        note_launches(w->stream, r.bwd_kernels);
     } else {
         rc = enqueue_rollout_backward(w, c);
         if (rc) return rc;

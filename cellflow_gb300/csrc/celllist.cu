@@ -540,6 +540,7 @@ cudaError_t launch_cell_hash(const float4* pos, int n, const Grid& g, const floa
     if (n <= 0) return cudaSuccess;
     cell_hash_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(pos, n, g, ext[0], ext[1], ext[2], num_types,
                                                                   keys, err);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -555,11 +556,15 @@ cudaError_t launch_scan_exclusive(const uint32_t* in, uint32_t* out, int n, uint
             if (e != cudaSuccess) return e;
         }
         scan_single_block<<<1, kThreads, 0, st>>>(out, n);
+        note_launches(st);
         return cudaGetLastError();
     }
     scan_tile_sums<<<tiles, kThreads, 0, st>>>(in, n, tmp);
+    note_launches(st);
     scan_single_block<<<1, kThreads, 0, st>>>(tmp, tiles);
+    note_launches(st);
     scan_apply<<<tiles, kThreads, 0, st>>>(in, out, n, tmp);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -577,18 +582,24 @@ cudaError_t launch_radix_sort(Scratch& s, int n, int key_bits, int* which, cudaS
     for (int p = 0; p < passes; p++) {
         int shift = 8 * p;
         const uint32_t* vals_in = p == 0 ? nullptr : s.vals[cur];
-        if (items == kSortItemsSmall)
+        if (items == kSortItemsSmall) {
             radix_hist_kernel<kSortItemsSmall><<<nblocks, kThreads, 0, st>>>(s.keys[cur], n, shift, s.hist, nblocks);
-        else
+            note_launches(st);
+        } else {
             radix_hist_kernel<kSortItemsLarge><<<nblocks, kThreads, 0, st>>>(s.keys[cur], n, shift, s.hist, nblocks);
+            note_launches(st);
+        }
         cudaError_t e = launch_scan_exclusive(s.hist, s.hist, (int)entries, s.scan_tmp, s.scan_tmp_cap, st);
         if (e != cudaSuccess) return e;
-        if (items == kSortItemsSmall)
+        if (items == kSortItemsSmall) {
             radix_scatter_kernel<kSortItemsSmall><<<nblocks, kThreads, 0, st>>>(
                 s.keys[cur], vals_in, s.keys[cur ^ 1], s.vals[cur ^ 1], n, shift, s.hist, nblocks);
-        else
+            note_launches(st);
+        } else {
             radix_scatter_kernel<kSortItemsLarge><<<nblocks, kThreads, 0, st>>>(
                 s.keys[cur], vals_in, s.keys[cur ^ 1], s.vals[cur ^ 1], n, shift, s.hist, nblocks);
+            note_launches(st);
+        }
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         cur ^= 1;
@@ -606,6 +617,7 @@ cudaError_t launch_cell_bounds(const uint32_t* keys, const uint32_t* vals, int n
     if (e != cudaSuccess) return e;
     if (n <= 0) return cudaSuccess;
     cell_bounds_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(keys, vals, n, pos, start, end, pos_sorted);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -637,15 +649,19 @@ cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const 
     cudaError_t e = cudaMemsetAsync(cell_off, 0, sizeof(uint32_t) * ((size_t)g.cells + 1), st);
     if (e != cudaSuccess) return e;
     const int tiles = cell_list_tiles(g);
-    if (n > 0)
+    if (n > 0) {
         cell_hash_count_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(
             pos, n, g, ext[0], ext[1], ext[2], num_types, s.keys[0], cell_off, tiles ? s.aux : nullptr, err);
+        note_launches(st);
+    }
     if (!tiles) {
         // rows longer than a tile: stable radix sort of the cell ids, device-wide scan
         e = launch_radix_sort(s, n, g.key_bits, which, st);
         if (e == cudaSuccess) e = launch_scan_exclusive(cell_off, cell_off, g.cells + 1, s.scan_tmp, s.scan_tmp_cap, st);
-        if (e == cudaSuccess && n > 0)
+        if (e == cudaSuccess && n > 0) {
             gather_sorted_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.vals[*which], n, pos, s.pos_sorted);
+            note_launches(st);
+        }
         if (e == cudaSuccess && items) e = launch_step_plan(cell_off, n, g, items, n_items, st);
         return e == cudaSuccess ? cudaGetLastError() : e;
     }
@@ -657,12 +673,16 @@ cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const 
     tg.rows_per_tile = tile_rows(g);
     tg.tiles = tiles;
     tile_reduce_kernel<<<tiles, kTileThreads, 0, st>>>(cell_off, tg, s.tile_sums);
+    note_launches(st);
     tile_apply_kernel<<<tiles, kTileThreads, 0, st>>>(cell_off, tg, s.tile_sums, items, n_items);
+    note_launches(st);
     *which = 1;
     if (n > 0) {
         place_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.keys[0], s.aux, cell_off, n, s.vals[0]);
+        note_launches(st);
         rank_gather_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.vals[0], s.keys[0], cell_off, pos, n,
                                                                          s.vals[1], s.keys[1], s.pos_sorted);
+        note_launches(st);
     }
     return cudaGetLastError();
 }
@@ -690,7 +710,9 @@ cudaError_t launch_work_counters(const float4* pos, const int* counts, int n, co
     if (e != cudaSuccess) return e;
     if (n <= 0) return cudaSuccess;
     population_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(pos, n, canon, pop);
+    note_launches(st);
     c27_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(pos, counts, n, canon, pop, out);
+    note_launches(st);
     return cudaGetLastError();
 }
 

@@ -172,6 +172,7 @@ struct Rollout {
     float radio[CF_MAX_TYPES] = {};
     // the backward as one CUDA graph, re-captured when its key changes
     cudaGraphExec_t bwd_graph = nullptr;
+    long long bwd_kernels = 0;  // kernel nodes of bwd_graph
     StepConsts bwd_key{};
     int bwd_steps = 0, bwd_every = 0;
     const void* bwd_bufs = nullptr;
@@ -187,6 +188,7 @@ constexpr int kGradAccEntries = kTableSize + 8;
 // mesh): cell list on its grid, selection kernel, scan, count read-back.
 struct SelGraph {
     cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;  // kernel nodes of exec
     Grid g{};
     float dsq = 0.0f;
     int max_conn = -1, n = -1, types = -1;
@@ -235,6 +237,7 @@ struct cf_world {
     // one-step CUDA graphs (index 1: with the profiling events), re-captured
     // when the step constants or buffers change
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    long long graph_kernels[2] = {0, 0};  // kernel nodes of graph[k]
     cf::StepConsts graph_key[2];
     const void* graph_bufs[2] = {nullptr, nullptr};
     bool use_graphs = true;
@@ -247,6 +250,7 @@ struct cf_world {
     // cf_step_host: upload, step and read-back as one graph, keyed by the step
     // constants, the host buffers and the scratch identity
     cudaGraphExec_t host_graph = nullptr;
+    long long host_graph_kernels = 0;
     cf::StepConsts host_key;
     const void* host_in = nullptr;
     void* host_out = nullptr;
@@ -259,6 +263,14 @@ namespace cf {
 // Error plumbing (thread-local message, see cf_last_error).
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
+
+// Launch tally: kernels this library has put on a stream since it was loaded.
+// Every launch site notes its kernel (nothing is counted while the stream is
+// being captured); a graph replay notes the kernel nodes of its graph.
+void note_launches(cudaStream_t st, long long k = 1);
+long long launch_tally();
+// Kernel nodes of a captured graph.
+cudaError_t graph_kernel_count(cudaGraph_t graph, long long* kernels);
 #define CF_CUDA(call)                                                   \
     do {                                                                \
         cudaError_t cf_e_ = (call);                                     \

@@ -96,6 +96,7 @@ cudaError_t launch_init_particles(float4* pos, float4* vel, float4* acc, int* co
     const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
     init_particles_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
         pos, vel, acc, counts, n, num_types, lo[0], lo[1], lo[2], span[0], span[1], span[2], key, world);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -103,6 +104,7 @@ cudaError_t launch_aos_to_soa(const cf_particle* aos, float4* pos, float4* vel, 
 {
     if (n <= 0) return cudaSuccess;
     aos_to_soa_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(aos, pos, vel, acc, n);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -111,6 +113,7 @@ cudaError_t launch_soa_to_aos(const float4* pos, const float4* vel, const float4
 {
     if (n <= 0) return cudaSuccess;
     soa_to_aos_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(pos, vel, acc, aos, n);
+    note_launches(st);
     return cudaGetLastError();
 }
 

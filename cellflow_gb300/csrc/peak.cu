@@ -49,6 +49,7 @@ extern "C" int cf_measure_fp32_peak(double* tflops)
     for (int rep = 0; rep < 6; rep++) {
         CF_CUDA(cudaEventRecord(e0, st));
         fma_chains_kernel<<<blocks, kThreads, 0, st>>>(out, 0.999999f, 1e-7f);
+        note_launches(st);
         CF_CUDA(cudaEventRecord(e1, st));
         CF_CUDA(cudaEventSynchronize(e1));
         float ms = 0.0f;

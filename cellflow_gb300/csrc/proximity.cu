@@ -303,6 +303,7 @@ cudaError_t launch_mesh_select(const float4* pos_sorted, const uint32_t* keys_so
     mesh_select_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted,
                                                                           cell_start, cell_end, g, n, dsq, max_conn,
                                                                           slots, count);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -313,6 +314,7 @@ cudaError_t launch_mesh_emit(const int32_t* slots, const uint32_t* offsets, int 
     if (n <= 0 || cap_tris <= 0) return cudaSuccess;
     mesh_emit_kernel<<<(n + 255) / 256, 256, 0, st>>>(slots, offsets, n, pos, colors, n_colors, tris, vertices,
                                                       cap_tris);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -323,12 +325,15 @@ cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* ke
 {
     if (n <= 0) return cudaSuccess;
     const int blocks = (n + kThreads - 1) / kThreads;
-    if (csr)
+    if (csr) {
         proximity_select_kernel<true><<<blocks, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted, cell_start,
                                                                   cell_end, g, n, dsq, max_conn, slots, count);
-    else
+        note_launches(st);
+    } else {
         proximity_select_kernel<false><<<blocks, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted, cell_start,
                                                                    cell_end, g, n, dsq, max_conn, slots, count);
+        note_launches(st);
+    }
     return cudaGetLastError();
 }
 
@@ -338,6 +343,7 @@ cudaError_t launch_proximity_emit_edges(const int32_t* slots, const uint32_t* of
     (void)max_conn;
     if (n <= 0 || cap <= 0) return cudaSuccess;
     proximity_edges_kernel<<<(n + 255) / 256, 256, 0, st>>>(slots, offsets, n, edges, cap);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -349,6 +355,7 @@ cudaError_t launch_proximity_emit_vertices(const int32_t* slots, const uint32_t*
     if (n <= 0 || cap_vertices <= 0) return cudaSuccess;
     proximity_vertices_kernel<<<(n + 255) / 256, 256, 0, st>>>(slots, offsets, n, pos, colors, n_colors, vertices,
                                                                cap_vertices);
+    note_launches(st);
     return cudaGetLastError();
 }
 

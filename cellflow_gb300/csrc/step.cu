@@ -681,6 +681,7 @@ cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const 
             CF_FORCE_LAUNCH(false, false);
     }
 #undef CF_FORCE_LAUNCH
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -695,6 +696,7 @@ cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, Ite
 {
     if (n <= 0) return cudaMemsetAsync(n_items, 0, sizeof(int), st);
     plan_kernel<<<1, 1024, 0, st>>>(cell_off, g.m[0], g.m[1], g.m[2], g.worlds * g.m[1] * g.m[2], items, n_items);
+    note_launches(st);
     return cudaGetLastError();
 }
 

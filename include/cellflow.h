@@ -103,6 +103,11 @@ typedef struct cf_device_view {
 
 const char* cf_last_error(void);
 const char* cf_version(void);
+/* Kernels this library has put on CUDA streams since it was loaded, all worlds
+ * and threads together: every direct launch, and every kernel node of each
+ * CUDA graph it launches (a step, a batch replay, a selection pass, a rollout
+ * backward).  The difference around a region is that region's launch count. */
+long long cf_kernel_launches(void);
 /* SimulationParams defaults (SimulationParams.h:15-29). */
 void cf_default_params(cf_step_params* p);
 
