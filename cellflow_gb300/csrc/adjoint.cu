@@ -518,10 +518,12 @@ cudaError_t launch_rdf(const float* ext, const Grid& g, int n, int T, int bins, 
     cudaError_t e = cudaMemsetAsync(acc, 0, sizeof(double) * H, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(type_count, 0, sizeof(unsigned long long) * CF_MAX_TYPES, st);
     if (e != cudaSuccess) return e;
-    // one warp per home, grid-stride; two blocks per SM keep the histogram flushes few
+    // one warp per home, grid-stride; up to eight blocks per SM while their histograms
+    // stay within 48 KB of shared memory (every block flushes its histogram once)
     const int warps_per_block = kAdjThreads / 32;
+    const int per_sm = (int)std::max<size_t>(1, std::min<size_t>(8, (48u << 10) / rdf_smem_bytes(T, bins)));
     if (n > 0) {
-        rdf_kernel<<<std::min((n + warps_per_block - 1) / warps_per_block, 2 * num_sms()), kAdjThreads,
+        rdf_kernel<<<std::min((n + warps_per_block - 1) / warps_per_block, per_sm * num_sms()), kAdjThreads,
                      rdf_smem_bytes(T, bins), st>>>(c, pos_sorted, keys_sorted, cell_off, acc, type_count);
         note_launches(st);
     }
