@@ -31,7 +31,11 @@
 //     displacement; pairs below a second bound (<= the exact test for every
 //     pair) interact for certain, and only the rare pairs between the two
 //     bounds (a band ~1e-6 wide) take the reference's exact test on the
-//     unshifted coordinates.  Interacting pairs add their force term.
+//     unshifted coordinates.  Interacting pairs add their force term.  In
+//     the lane-paired variant the lanes are sorted by hit count and paired
+//     busiest with idlest; the idler lane of a pair, after its own hits,
+//     walks the top part of its partner's with its partner's home and hands
+//     the partial sums over, so the trip count falls towards the mean.
 //
 // Exactness (cuda-native/src/ParticleSimulation.cu:86-165):
 //   - the neighbour test is the reference's: d^2 = (dx*dx + dy*dy) + dz*dz and
@@ -48,6 +52,7 @@
 //   - force terms use rsqrt and exp approximations (a few ulp) and the
 //     contracted distance; the sum runs in cell order.
 //   The density factor, integrator and wrap are the reference's operations.
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "cf_internal.hpp"
@@ -111,14 +116,27 @@ __device__ __forceinline__ void stencil_origin(int clo, int chi, float cs, float
     }
 }
 
+// Lane pairing scratch of the drain (the variants that pair lanes):
+// each lane's home and filter operands for the pass, its group bitmap for the
+// batch, its partner, and its own partial sums while it works on its partner's hits.
+struct PairScratch {
+    float4 home_h[32];
+    float4 home_m2[32];
+    float4 saved[32];
+    uint32_t nzw[32];
+    uint32_t pairing[32];
+};
+struct NoScratch {};
+
 // Per-warp staging area, kStage candidates (a multiple of 32) per batch.
-template <int kStage>
+template <int kStage, bool kPairs>
 struct WarpSmem {
     float4 xy[kStage / 2];              // staged (x_a, x_b, y_a, y_b) of slots 2p, 2p+1
     float4 zc[kStage / 2];              // staged (z_a, z_b, |c_a|^2, |c_b|^2)
     uint32_t meta[kStage];              // sorted index | type << 27
     uint32_t mask[(kStage / 32) * 32];  // [group][lane]
     float origin[4];                    // the pass's staging origin (x, y, z)
+    typename std::conditional<kPairs, PairScratch, NoScratch>::type pr;
 };
 
 // Named barrier of the warps sharing an item: id 1 + slot (slot < kWarps),
@@ -236,7 +254,7 @@ __device__ __forceinline__ void staged_xyz(const float* xyf, const float* zcf, i
     z = zcf[pb];
 }
 
-template <int kStage, int kMinBlocks, bool kGeneric, bool kUniformR>
+template <int kStage, int kMinBlocks, bool kPairs, bool kGeneric, bool kUniformR>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
     step_force_kernel(StepConsts c, const PairTables* __restrict__ tables, const float4* __restrict__ pos_sorted,
                       const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ vals_sorted,
@@ -254,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     // force coefficients, compact T-stride: one copy per block for a single
     // world, one per warp (filled once its item's world is known) for a batch
     const bool one_world = c.grid.worlds == 1;
-    float2* coef_base = reinterpret_cast<float2*>(s_dyn + sizeof(WarpSmem<kStage>) * kWarps);
+    float2* coef_base = reinterpret_cast<float2*>(s_dyn + sizeof(WarpSmem<kStage, kPairs>) * kWarps);
     if (!kUniformR) {
         for (int e = threadIdx.x; e < T * T; e += kThreads) {
             const int a = e / T, b = e - a * T;
@@ -278,6 +296,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const float c1u = c.neg_k * kLog2e * c.inv_eff_uniform * c.inv_eff_uniform;
     // pairs per drain trip: two side by side where the register budget allows
     constexpr int kPer = kMinBlocks >= 8 ? 1 : 2;
+    // lane pairing in the drain (regular grids)
+    constexpr bool kBalance = kPairs && !kGeneric;
 
     // c.split warps (1, 2 or 4) share an item, each taking an equal share of its
     // candidates; part 0 adds the others' partial sums and integrates
@@ -286,7 +306,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const int part = warp & (split - 1);
     const int item = blockIdx.x * (kWarps / split) + warp / split;
     if (item >= *n_items) return;  // the item's other warps leave too: no barrier is pending
-    WarpSmem<kStage>& w = reinterpret_cast<WarpSmem<kStage>*>(s_dyn)[warp];
+    using Smem = WarpSmem<kStage, kPairs>;
+    Smem& w = reinterpret_cast<Smem*>(s_dyn)[warp];
     float2* wcoef = coef_base + (one_world ? 0 : warp * T * T);
     const float* xyf = reinterpret_cast<const float*>(w.xy);
     const float* zcf = reinterpret_cast<const float*>(w.zc);
@@ -361,6 +382,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 w.origin[0] = ox;
                 w.origin[1] = oy;
                 w.origin[2] = oz;
+            }
+            if constexpr (kBalance) {
+                w.pr.home_h[lane] = L.h;
+                w.pr.home_m2[lane] = make_float4(H.m2x.x, H.m2y.x, H.m2z.x, 0.0f);
             }
         } else {
             H.m2x = H.m2y = H.m2z = H.k = make_float2(0.0f, 0.0f);
@@ -516,20 +541,98 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             // lowest remaining bit of nz) with one load: no nested loop, no vote per trip.
             // A lane with fewer than kPer hits left repeats its first pair of the trip
             // without accumulating it.
-            const int trips = (__reduce_max_sync(0xffffffffu, hits) + kPer - 1) / kPer;
+            //
+            // Lane pairing (kBalance): the trip count is the busiest lane's, so lanes are
+            // paired heaviest with lightest (a bitonic sort of the hit counts) and the light
+            // lane of a pair, once its own hits are done (rounded up to a whole trip), takes
+            // the top part of its partner's hits with its partner's home, accumulating them
+            // apart; the partner adds that partial after the trips.  Each pair's work is then
+            // about half its total.
+            int upto = hits;         // pair indices below upto are valid in the current phase
+            int work = hits;         // pairs this lane walks in the batch
+            int switch_trip = -1;    // trip at which a light lane turns to its partner's hits
+            int partner = lane, fw = 0, src = lane;
+            bool light = false;
+            int fgi = 0;             // where a light lane's share of its partner's hits starts
+            uint32_t fm = 0u, fnz = 0u;
+            if constexpr (kBalance) {
+                uint32_t key = ((uint32_t)hits << 5) | (uint32_t)lane;
+#pragma unroll
+                for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+                    for (int j = k >> 1; j > 0; j >>= 1) {
+                        const uint32_t o = __shfl_xor_sync(0xffffffffu, key, j);
+                        key = (((lane & j) == 0) == ((lane & k) == 0)) ? min(key, o) : max(key, o);
+                    }
+                }
+                // sorted position lane holds key; it pairs with position 31 - lane
+                const uint32_t mate = __shfl_sync(0xffffffffu, key, 31 - lane);
+                w.pr.pairing[key & 31u] = (mate & 31u) | (lane < 16 ? 0x100u : 0u);
+                w.pr.nzw[lane] = nz;
+                __syncwarp();
+                const uint32_t pr = w.pr.pairing[lane];
+                partner = (int)(pr & 31u);
+                light = (pr & 0x100u) != 0u;
+                const int hp = __shfl_sync(0xffffffffu, hits, partner);
+                if (light) {
+                    const int padded = (hits + kPer - 1) / kPer * kPer;
+                    fw = max(0, (hp - padded) >> 1);
+                    work = padded + fw;
+                    if (fw > 0) {
+                        switch_trip = padded / kPer;
+                        // skip the partner's own share, its first hp - fw set bits; the group
+                        // bitmap keeps the current group as its lowest bit, like nz
+                        int skip = hp - fw;
+                        fnz = w.pr.nzw[partner];
+                        while (fnz) {
+                            fgi = __ffs(fnz) - 1;
+                            fm = w.mask[fgi * 32 + partner];
+                            const int cnt = __popc(fm);
+                            if (skip < cnt) break;
+                            skip -= cnt;
+                            fnz &= fnz - 1u;
+                        }
+                        for (; skip > 0; skip--) fm &= fm - 1u;
+                    }
+                } else {
+                    fw = max(0, (hits - (hp + kPer - 1) / kPer * kPer) >> 1);
+                    upto = work = hits - fw;
+                }
+            }
+            const int trips = (__reduce_max_sync(0xffffffffu, work) + kPer - 1) / kPer;
             int gi = nz ? __ffs(nz) - 1 : 0;
             uint32_t m = w.mask[gi * 32 + lane];
             for (int it = 0; it < trips; it++) {
-                if (kPer * it < hits) {
+                if constexpr (kBalance) {
+                    if (it == switch_trip) {
+                        // own hits done: keep their sums, take the partner's home and its top fw hits
+                        w.pr.saved[lane] = make_float4(L.fx, L.fy, L.fz, __int_as_float(L.count));
+                        L.fx = L.fy = L.fz = 0.0f;
+                        L.count = 0;
+                        const float4 ph = w.pr.home_h[partner];
+                        const float4 pm = w.pr.home_m2[partner];
+                        L.h = ph;
+                        L.tp = __float_as_uint(ph.w) & kTypeMask;
+                        H.m2x.x = pm.x;
+                        H.m2y.x = pm.y;
+                        H.m2z.x = pm.z;
+                        src = partner;
+                        gi = fgi;
+                        m = fm;
+                        nz = fnz;
+                        upto = kPer * it + fw;
+                    }
+                }
+                if (kPer * it < upto) {
                     int slot[kPer];
                     bool valid[kPer];
 #pragma unroll
                     for (int q = 0; q < kPer; q++) {
-                        valid[q] = kPer * it + q < hits;
+                        valid[q] = kPer * it + q < upto;
                         if (valid[q] && m == 0u) {
                             nz &= nz - 1u;
                             gi = __ffs(nz) - 1;  // a later group holds a hit
-                            m = w.mask[gi * 32 + lane];
+                            m = w.mask[gi * 32 + src];
                         }
                         slot[q] = valid[q] ? gi * 32 + (__ffs(m) - 1) : slot[0];
                         if (valid[q]) m &= m - 1u;
@@ -557,6 +660,33 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                             L.fz = fmaf(dz[q], wgt[q], L.fz);
                         }
                     }
+                }
+            }
+            if constexpr (kBalance) {
+                // a light lane that switched holds its partner's partial: hand it over and
+                // take back its own sums and home
+                const float px = __shfl_sync(0xffffffffu, L.fx, partner);
+                const float py = __shfl_sync(0xffffffffu, L.fy, partner);
+                const float pz = __shfl_sync(0xffffffffu, L.fz, partner);
+                const int pc = __shfl_sync(0xffffffffu, L.count, partner);
+                if (switch_trip >= 0) {
+                    const float4 sv = w.pr.saved[lane];
+                    L.fx = sv.x;
+                    L.fy = sv.y;
+                    L.fz = sv.z;
+                    L.count = __float_as_int(sv.w);
+                    const float4 oh = w.pr.home_h[lane];
+                    const float4 om = w.pr.home_m2[lane];
+                    L.h = oh;
+                    L.tp = __float_as_uint(oh.w) & kTypeMask;
+                    H.m2x.x = om.x;
+                    H.m2y.x = om.y;
+                    H.m2z.x = om.z;
+                } else if (!light && fw > 0) {
+                    L.fx += px;
+                    L.fy += py;
+                    L.fz += pz;
+                    L.count += pc;
                 }
             }
             __syncwarp();
@@ -638,36 +768,36 @@ __global__ void __launch_bounds__(1024)
     if (tid == 1023) *n_items = (int)s_chunk[1023];
 }
 
-template <int S, int B, bool G, bool U>
+template <int S, int B, bool P, bool G, bool U>
 cudaError_t configure_one()
 {
-    return cudaFuncSetAttribute(step_force_kernel<S, B, G, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)((sizeof(WarpSmem<S>) + sizeof(float2) * kTableSize) * kWarps));
+    return cudaFuncSetAttribute(step_force_kernel<S, B, P, G, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)((sizeof(WarpSmem<S, P>) + sizeof(float2) * kTableSize) * kWarps));
 }
 
-template <int S, int B>
+template <int S, int B, bool P>
 cudaError_t configure_variant()
 {
-    cudaError_t e = configure_one<S, B, false, false>();
-    if (e == cudaSuccess) e = configure_one<S, B, false, true>();
-    if (e == cudaSuccess) e = configure_one<S, B, true, false>();
-    if (e == cudaSuccess) e = configure_one<S, B, true, true>();
+    cudaError_t e = configure_one<S, B, P, false, false>();
+    if (e == cudaSuccess) e = configure_one<S, B, P, false, true>();
+    if (e == cudaSuccess) e = configure_one<S, B, P, true, false>();
+    if (e == cudaSuccess) e = configure_one<S, B, P, true, true>();
     return e;
 }
 
 // Variant S = staged candidates per batch, B = resident blocks per SM the
-// register budget is sized for.
-template <int S, int B>
+// register budget is sized for, P = lanes paired in the drain.
+template <int S, int B, bool P>
 cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
                            const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
                            const Item* items, const int* n_items, int blocks, float4* pos, float4* vel, float4* acc,
                            int* counts, cudaStream_t st)
 {
     // staging per warp; force coefficients per block (one world) or per warp (a batch)
-    const size_t smem = sizeof(WarpSmem<S>) * kWarps +
+    const size_t smem = sizeof(WarpSmem<S, P>) * kWarps +
                         sizeof(float2) * c.num_types * c.num_types * (c.grid.worlds == 1 ? 1 : kWarps);
 #define CF_FORCE_LAUNCH(G, U)                                                                                        \
-    step_force_kernel<S, B, G, U><<<blocks, kThreads, smem, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted,   \
+    step_force_kernel<S, B, P, G, U><<<blocks, kThreads, smem, st>>>(c, tables, pos_sorted, keys_sorted, vals_sorted,   \
                                                                   cell_off, items, n_items, pos, vel, acc, counts)
     if (c.grid.generic) {
         if (c.uniform_r)
@@ -704,10 +834,10 @@ cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, Ite
 // stream capture).
 cudaError_t configure_step_force()
 {
-    cudaError_t e = configure_variant<256, 8>();
-    if (e == cudaSuccess) e = configure_variant<256, 6>();
-    if (e == cudaSuccess) e = configure_variant<512, 4>();
-    if (e == cudaSuccess) e = configure_variant<384, 6>();
+    cudaError_t e = configure_variant<256, 8, false>();
+    if (e == cudaSuccess) e = configure_variant<256, 6, false>();
+    if (e == cudaSuccess) e = configure_variant<256, 6, true>();
+    if (e == cudaSuccess) e = configure_variant<384, 6, false>();
     return e;
 }
 
@@ -721,16 +851,16 @@ cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, con
     const int blocks = (int)(((long long)max_items * c.split + kWarps - 1) / kWarps);
     switch (c.variant) {
     case 1:
-        return launch_variant<256, 6>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+        return launch_variant<256, 6, false>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
                                       blocks, pos, vel, acc, counts, st);
     case 2:
-        return launch_variant<512, 4>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+        return launch_variant<256, 6, true>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
                                       blocks, pos, vel, acc, counts, st);
     case 3:
-        return launch_variant<384, 6>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+        return launch_variant<384, 6, false>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
                                       blocks, pos, vel, acc, counts, st);
     default:
-        return launch_variant<256, 8>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+        return launch_variant<256, 8, false>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
                                       blocks, pos, vel, acc, counts, st);
     }
 }

@@ -197,12 +197,14 @@ int cf_step_host(cf_world* w, const cf_step_params* p, const cf_particle* in, cf
 
 /* Force-kernel variants: v % 4 picks the staging: 0 = 256 candidates staged
  * per warp batch, register budget for 8 blocks per SM; 1 = 256 staged, 6
- * blocks per SM; 2 = 512 staged, 4 blocks per SM; 3 = 384 staged, 6 blocks
- * per SM.  v / 4 picks the warps per 32-particle item: 1, 2 or 4 (each warp
- * takes an equal share of the item's candidates; more warps for worlds too
- * small to fill the GPU).  Results are bit-identical across stagings; with
- * 2 or 4 warps the partial sums are added in a fixed order, which differs
- * from the single-warp order by rounding only. */
+ * blocks per SM; 2 = as 1 with lanes paired in the drain (the lane with the
+ * fewest hits of a batch takes part of the busiest lane's, and so on down the
+ * sorted hit counts); 3 = 384 staged, 6 blocks per SM.  v / 4 picks the warps
+ * per 32-particle item: 1, 2 or 4 (each warp takes an equal share of the
+ * item's candidates; more warps for worlds too small to fill the GPU).
+ * Results are bit-identical across stagings 0, 1 and 3; with lane pairing,
+ * and with 2 or 4 warps, partial sums are added in a fixed order, which
+ * differs from the single-lane order by rounding only. */
 #define CF_FORCE_VARIANTS 12
 /* Autotuner of the step (no counterpart in the reference): runs `steps`
  * trial steps with each force-kernel variant, restores the particle state,
