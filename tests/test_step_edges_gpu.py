@@ -1,7 +1,8 @@
 """Edge cases of the GPU step against the oracle: empty and single-particle worlds,
 particles on the box faces and pairs across the periodic boundary at the interaction
 threshold, every particle in one cell, rows of 4096 cells (one row per tile of the cell
-list), and items split over several warps when a world has a single item."""
+list), items split over several warps when a world has a single item, and dense blobs
+under the lane-paired drain."""
 
 import numpy as np
 import pytest
@@ -155,3 +156,19 @@ def test_single_item_world_under_every_variant(cflib, variant):
     rec, counts = step_vs_oracle(pos, w.types(), w.table(), params_for(3, 0.3), variant=variant,
                                  label=f"tiny, variant {variant}")
     assert counts.min() == 19
+
+
+@pytest.mark.parametrize("variant", [1, 2, 6, 10])
+def test_skewed_occupancy_under_lane_pairing(cflib, variant):
+    """Dense Gaussian blobs (hundreds of neighbours next to a few): the lanes of an item have
+    very uneven hit counts, so the lane-paired drain (stagings 2: variants 2, 6, 10) hands
+    large parts of busy lanes' hits to idle ones; counts stay bit-exact and forces within
+    the step tolerance, as with the unpaired staging (variant 1)."""
+    n, T = 12000, 5
+    pos = inputs.blob_positions(n, 6, 0.04, 0x5EED0031)
+    types = inputs.uniform_types(n, T, 0x5EED0031)
+    table = inputs.gaussian_table(T, 0.1, 0.6, 0x5EED0031)
+    rec, counts = step_vs_oracle(pos, types, table, params_for(T, 0.05), variant=variant,
+                                 label=f"blobs, variant {variant}")
+    med = np.median(counts)
+    assert counts.max() > 2 * med and counts.min() < med / 4
