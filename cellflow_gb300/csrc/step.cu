@@ -294,8 +294,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     }
     __syncthreads();
     const float c1u = c.neg_k * kLog2e * c.inv_eff_uniform * c.inv_eff_uniform;
-    // pairs per drain trip: two side by side where the register budget allows
-    constexpr int kPer = kMinBlocks >= 8 ? 1 : 2;
+    // pairs per drain trip: two side by side where the register budget allows,
+    // three with lane pairing (more of the lanes stay busy, so more independent
+    // work per trip pays there; it does not without pairing)
+    constexpr int kPer = kMinBlocks >= 8 ? 1 : (kPairs && !kGeneric ? 3 : 2);
     // lane pairing in the drain (regular grids)
     constexpr bool kBalance = kPairs && !kGeneric;
 
