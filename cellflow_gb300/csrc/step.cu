@@ -26,10 +26,11 @@
 //     shifted into a 32-bit mask per 32 candidates.  The bound is >= the
 //     exact test for every pair plus the expansion's rounding, which the
 //     origin keeps at the scale of the stencil box.  ~85% of pairs stop here.
-//   Drain: for every set bit (two per trip, a warp-uniform trip count from
-//     the filter's per-lane hit counts), the contracted distance of the
-//     displacement; pairs below a second bound (<= the exact test for every
-//     pair) interact for certain, and only the rare pairs between the two
+//   Drain: for every set bit (two per trip, three with lane pairing; a
+//     warp-uniform trip count from the filter's per-lane hit counts), the
+//     contracted distance of the displacement; pairs below a second bound
+//     (<= the exact test for every pair) interact for certain, and only the
+//     rare pairs between the two
 //     bounds (a band ~1e-6 wide) take the reference's exact test on the
 //     unshifted coordinates.  Interacting pairs add their force term.  In
 //     the lane-paired variant the lanes are sorted by hit count and paired
