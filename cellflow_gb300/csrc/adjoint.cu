@@ -129,6 +129,58 @@ __device__ __forceinline__ void x_runs(int cx, int m0, int& a0, int& b0, int& a1
     }
 }
 
+constexpr int kListCap = 256;  // candidate indices staged per warp at a time
+
+// Calls fn(q) for every particle q in the 27-cell stencil of cell `cell` (fewer
+// cells on axes under 3 cells), spread over the lanes of the calling warp.  The
+// stencil's rows are at most 18 runs of consecutive cells, i.e. contiguous ranges
+// of the sorted snapshot; lane r < 18 describes run r, a warp prefix sum
+// concatenates them, and the concatenation is staged kListCap indices at a time
+// into the warp's list, so the lanes stride over the whole candidate set rather
+// than over one short run at a time.  The whole warp calls it; fn must not
+// synchronise the warp.
+template <typename Fn>
+__device__ __forceinline__ void for_stencil(int m0, int m1, int m2, uint32_t cell,
+                                            const uint32_t* __restrict__ cell_off, uint32_t* list, int lane, Fn fn)
+{
+    const int cx = (int)(cell % (uint32_t)m0), cy = (int)((cell / (uint32_t)m0) % (uint32_t)m1),
+              cz = (int)(cell / ((uint32_t)m0 * (uint32_t)m1));
+    int ylo, yhi, zlo, zhi, a0, b0, a1, b1;
+    axis_range(m1, ylo, yhi);
+    axis_range(m2, zlo, zhi);
+    x_runs(cx, m0, a0, b0, a1, b1);
+    const int ny = yhi - ylo + 1, nrows = ny * (zhi - zlo + 1);
+    uint32_t beg = 0u;
+    int len = 0;
+    if (lane < 2 * nrows) {
+        const int r = lane >> 1, run = lane & 1;
+        const int oy = ylo + r % ny, oz = zlo + r / ny;
+        const int ra = run ? a1 : a0, rb = run ? b1 : b0;
+        if (rb >= ra) {
+            const int row = (wrap_cell(cz + oz, m2) * m1 + wrap_cell(cy + oy, m1)) * m0;
+            beg = cell_off[row + ra];
+            len = (int)(cell_off[row + rb + 1] - beg);
+        }
+    }
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int pre = incl - len;
+    for (int base = 0; base < total; base += kListCap) {
+        // every run writes its part of [base, base + kListCap)
+        const int j0 = max(0, base - pre), j1 = min(len, base + kListCap - pre);
+        for (int j = j0; j < j1; j++) list[pre + j - base] = beg + (uint32_t)j;
+        __syncwarp();
+        const int lim = min(kListCap, total - base);
+        for (int g = lane; g < lim; g += 32) fn(list[g]);
+        __syncwarp();
+    }
+}
+
 // One warp per home particle (grid-stride over homes in cell order): the
 // lanes share the home's 27-cell stencil, nine rows of at most two runs of
 // consecutive cells, i.e. contiguous ranges of the sorted snapshot, and
@@ -144,6 +196,7 @@ __global__ void __launch_bounds__(kAdjThreads)
     __shared__ float s_gF[kTableSize];
     __shared__ float s_par[8];
     __shared__ float s_thr[kTableSize], s_inv_eff[kTableSize], s_F[kTableSize];
+    __shared__ uint32_t s_list[kAdjThreads / 32][kListCap];
     for (int q = threadIdx.x; q < kTableSize; q += blockDim.x) {
         s_gF[q] = 0.0f;
         s_thr[q] = tables->threshold[q];
@@ -159,30 +212,17 @@ __global__ void __launch_bounds__(kAdjThreads)
     const int warps = (int)(gridDim.x * (blockDim.x >> 5));
     const float R = c.repulsion, A = c.attraction;
     const int m0 = c.grid.m[0], m1 = c.grid.m[1], m2 = c.grid.m[2];
-    int ylo, yhi, zlo, zhi;
-    axis_range(m1, ylo, yhi);
-    axis_range(m2, zlo, zhi);
+    uint32_t* list = s_list[threadIdx.x >> 5];
     float pR = 0.0f, pA = 0.0f, pK = 0.0f, pM = 0.0f, pB = 0.0f;
     for (int k = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); k < c.n; k += warps) {
         const float4 h = pos_sorted[k];
         const uint32_t ti = type_of(h);
         const float4 gfi = gf_sorted[k];
         const uint32_t cell = keys[k];
-        const int cx = (int)(cell % (uint32_t)m0), cy = (int)((cell / (uint32_t)m0) % (uint32_t)m1),
-                  cz = (int)(cell / ((uint32_t)m0 * (uint32_t)m1));
-        int a0, b0, a1, b1;
-        x_runs(cx, m0, a0, b0, a1, b1);
         float ax = 0.0f, ay = 0.0f, az = 0.0f;  // pair part of gx_i
         float fx = 0.0f, fy = 0.0f, fz = 0.0f;  // unscaled force f_i
-        for (int oz = zlo; oz <= zhi; oz++)
-            for (int oy = ylo; oy <= yhi; oy++) {
-                const int row = (wrap_cell(cz + oz, m2) * m1 + wrap_cell(cy + oy, m1)) * m0;
-                for (int run = 0; run < 2; run++) {
-                    const int ra = run ? a1 : a0, rb = run ? b1 : b0;
-                    if (rb < ra) continue;
-                    const uint32_t qb = cell_off[row + ra], qe = cell_off[row + rb + 1];
-                    for (uint32_t q = qb + lane; q < qe; q += 32) {
-                        if ((int)q == k) continue;
+        for_stencil(m0, m1, m2, cell, cell_off, list, lane, [&](uint32_t q) {
+                        if ((int)q == k) return;
                         const float4 o = pos_sorted[q];
                         // the reference's displacement and neighbour test (ParticleSimulation.cu:97-111)
                         const float dx = wrap_ref(__fsub_rn(o.x, h.x), c.ext[0], c.half[0]);
@@ -193,7 +233,7 @@ __global__ void __launch_bounds__(kAdjThreads)
                         const float s = __fadd_rn(d2, 0.0001f);
                         const uint32_t tj = type_of(o);
                         const int pair = ti * kTableStride + tj;
-                        if (!(s < s_thr[pair])) continue;
+                        if (!(s < s_thr[pair])) return;
                         // rsqrt and exp2 approximations (a few ulp): the gradient's tolerance
                         // is far wider than the forward's
                         const float inv_eff = s_inv_eff[pair];
@@ -223,9 +263,7 @@ __global__ void __launch_bounds__(kAdjThreads)
                         fx += fw * dx;
                         fy += fw * dy;
                         fz += fw * dz;
-                    }
-                }
-            }
+        });
         ax = warp_sum(ax);
         ay = warp_sum(ay);
         az = warp_sum(az);
@@ -301,40 +339,22 @@ __device__ __forceinline__ float bspline3_d(float t)
 }
 
 // Calls fn(q, o, dx, dy, dz, r) for every other particle q (position o) within r_cut of
-// home k. A warp shares the walk: its lanes stride over each stencil row's particles (at
-// most two runs of consecutive cells per row, contiguous ranges of the sorted snapshot).
+// home k, spread over the lanes of the calling warp (for_stencil).
 template <typename Fn>
 __device__ __forceinline__ void rdf_neighbours_warp(const RdfConsts& c, const float4* __restrict__ pos_sorted,
                                                     const uint32_t* __restrict__ keys,
-                                                    const uint32_t* __restrict__ cell_off, int k, const float4& h,
-                                                    int lane, Fn fn)
+                                                    const uint32_t* __restrict__ cell_off, uint32_t* list, int k,
+                                                    const float4& h, int lane, Fn fn)
 {
-    const int m0 = c.m[0], m1 = c.m[1], m2 = c.m[2];
-    const uint32_t cell = keys[k];
-    const int cx = (int)(cell % (uint32_t)m0), cy = (int)((cell / (uint32_t)m0) % (uint32_t)m1),
-              cz = (int)(cell / ((uint32_t)m0 * (uint32_t)m1));
-    int ylo, yhi, zlo, zhi, a0, b0, a1, b1;
-    axis_range(m1, ylo, yhi);
-    axis_range(m2, zlo, zhi);
-    x_runs(cx, m0, a0, b0, a1, b1);
-    for (int oz = zlo; oz <= zhi; oz++)
-        for (int oy = ylo; oy <= yhi; oy++) {
-            const int row = (wrap_cell(cz + oz, m2) * m1 + wrap_cell(cy + oy, m1)) * m0;
-            for (int run = 0; run < 2; run++) {
-                const int ra = run ? a1 : a0, rb = run ? b1 : b0;
-                if (rb < ra) continue;
-                const uint32_t qb = cell_off[row + ra], qe = cell_off[row + rb + 1];
-                for (uint32_t q = qb + lane; q < qe; q += 32) {
-                    if ((int)q == k) continue;
-                    const float4 o = pos_sorted[q];
-                    const float dx = wrap_ref(o.x - h.x, c.ext[0], c.half[0]);
-                    const float dy = wrap_ref(o.y - h.y, c.ext[1], c.half[1]);
-                    const float dz = wrap_ref(o.z - h.z, c.ext[2], c.half[2]);
-                    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-                    if (r < c.r_cut) fn(q, o, dx, dy, dz, r);
-                }
-            }
-        }
+    for_stencil(c.m[0], c.m[1], c.m[2], keys[k], cell_off, list, lane, [&](uint32_t q) {
+        if ((int)q == k) return;
+        const float4 o = pos_sorted[q];
+        const float dx = wrap_ref(o.x - h.x, c.ext[0], c.half[0]);
+        const float dy = wrap_ref(o.y - h.y, c.ext[1], c.half[1]);
+        const float dz = wrap_ref(o.z - h.z, c.ext[2], c.half[2]);
+        const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+        if (r < c.r_cut) fn(q, o, dx, dy, dz, r);
+    });
 }
 
 // One warp per home (grid-stride), the histogram in shared memory per block.
@@ -344,6 +364,7 @@ __global__ void rdf_kernel(RdfConsts c, const float4* __restrict__ pos_sorted, c
 {
     extern __shared__ float s_hist[];
     __shared__ unsigned int s_count[CF_MAX_TYPES];
+    __shared__ uint32_t s_list[kAdjThreads / 32][kListCap];
     const int H = c.T * c.T * c.bins;
     for (int q = threadIdx.x; q < H; q += blockDim.x) s_hist[q] = 0.0f;
     if (threadIdx.x < CF_MAX_TYPES) s_count[threadIdx.x] = 0u;
@@ -356,7 +377,7 @@ __global__ void rdf_kernel(RdfConsts c, const float4* __restrict__ pos_sorted, c
         // a type outside [0, T) is reported by the cell list's hash; skip it here
         if (ti >= (uint32_t)c.T) continue;
         if (lane == 0) atomicAdd(&s_count[ti], 1u);
-        rdf_neighbours_warp(c, pos_sorted, keys, cell_off, k, h, lane,
+        rdf_neighbours_warp(c, pos_sorted, keys, cell_off, s_list[threadIdx.x >> 5], k, h, lane,
                             [&](uint32_t, const float4& o, float, float, float, float r) {
                                 if (type_of(o) >= (uint32_t)c.T) return;
                                 const float t0 = r * c.inv_bin - 0.5f;
@@ -407,6 +428,7 @@ __global__ void rdf_grad_kernel(RdfConsts c, const float4* __restrict__ pos_sort
                                 float4* __restrict__ gpos)
 {
     extern __shared__ float s_g[];  // ghist / den
+    __shared__ uint32_t s_list[kAdjThreads / 32][kListCap];
     const int H = c.T * c.T * c.bins;
     for (int q = threadIdx.x; q < H; q += blockDim.x) {
         const double den = rdf_den(c, type_count, q);
@@ -421,7 +443,7 @@ __global__ void rdf_grad_kernel(RdfConsts c, const float4* __restrict__ pos_sort
         float ax = 0.0f, ay = 0.0f, az = 0.0f;
         // a type outside [0, T) is reported by the cell list's hash; it contributes nothing here
         if (ti < (uint32_t)c.T)
-            rdf_neighbours_warp(c, pos_sorted, keys, cell_off, k, h, lane,
+            rdf_neighbours_warp(c, pos_sorted, keys, cell_off, s_list[threadIdx.x >> 5], k, h, lane,
                                 [&](uint32_t, const float4& o, float dx, float dy, float dz, float r) {
                                     const uint32_t tj = type_of(o);
                                     if (!(r > 0.0f) || tj >= (uint32_t)c.T) return;
