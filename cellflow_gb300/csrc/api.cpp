@@ -114,6 +114,9 @@ void free_rollout(cf_world* w)
 {
     Rollout& r = w->ro;
     if (r.bwd_graph) cudaGraphExecDestroy(r.bwd_graph);
+    if (r.ev_fork) cudaEventDestroy(r.ev_fork);
+    if (r.ev_join) cudaEventDestroy(r.ev_join);
+    if (r.side) cudaStreamDestroy(r.side);
     for (void* p : {(void*)r.ckpt_pos, (void*)r.ckpt_vel, (void*)r.ckpt_cnt, (void*)r.seg_pos, (void*)r.seg_vel,
                     (void*)r.seg_cnt, (void*)r.fin_pos, (void*)r.fin_vel, (void*)r.fin_cnt, (void*)r.gx,
                     (void*)r.gv, (void*)r.gf_sorted, (void*)r.ga_sorted, (void*)r.gacc, (void*)r.rdf_pos,
@@ -1880,9 +1883,9 @@ int ensure_rollout(cf_world* w, int ckpts, int seg_states)
     CF_CUDA(dev_alloc(&r.ckpt_pos, nn * ck));
     CF_CUDA(dev_alloc(&r.ckpt_vel, nn * ck));
     CF_CUDA(dev_alloc(&r.ckpt_cnt, nn * ck));
-    CF_CUDA(dev_alloc(&r.seg_pos, nn * sg));
-    CF_CUDA(dev_alloc(&r.seg_vel, nn * sg));
-    CF_CUDA(dev_alloc(&r.seg_cnt, nn * sg));
+    CF_CUDA(dev_alloc(&r.seg_pos, nn * sg * 2));
+    CF_CUDA(dev_alloc(&r.seg_vel, nn * sg * 2));
+    CF_CUDA(dev_alloc(&r.seg_cnt, nn * sg * 2));
     CF_CUDA(dev_alloc(&r.fin_pos, nn));
     CF_CUDA(dev_alloc(&r.fin_vel, nn));
     CF_CUDA(dev_alloc(&r.fin_cnt, nn));
@@ -1909,11 +1912,11 @@ int ensure_rollout_lists(cf_world* w, int steps, int cells)
     r.seg_keys = r.seg_vals = r.seg_off = nullptr;
     r.lists_steps = 0;
     r.lists_cells = 0;
-    const size_t nn = (size_t)std::max(w->n, 1) * (size_t)steps;
+    const size_t nn = (size_t)std::max(w->n, 1) * (size_t)steps * 2;
     CF_CUDA(dev_alloc(&r.seg_sorted, nn));
     CF_CUDA(dev_alloc(&r.seg_keys, nn));
     CF_CUDA(dev_alloc(&r.seg_vals, nn));
-    CF_CUDA(dev_alloc(&r.seg_off, offs * (size_t)steps));
+    CF_CUDA(dev_alloc(&r.seg_off, offs * (size_t)steps * 2));
     r.lists_steps = steps;
     r.lists_cells = offs;
     return CF_OK;
@@ -1946,66 +1949,140 @@ int copy_state(cf_world* w, float4* dp, float4* dv, int* dc, const float4* sp, c
 // state, and run the adjoint steps of the segment in reverse; restore the
 // final state.  gx / gv hold dL/dx_K and dL/dv_K on entry, dL/dx_0 and
 // dL/dv_0 on exit; gacc collects the parameter gradients.
-int enqueue_rollout_backward(cf_world* w, const StepConsts& c)
+// Segment buffer `buf` (0 or 1) of the replayed states and cell lists.
+struct SegBuf {
+    float4 *pos, *vel, *sorted;
+    int* cnt;
+    uint32_t *keys, *vals, *off;
+};
+
+SegBuf seg_buf(const Rollout& r, size_t n, int buf)
+{
+    const size_t states = (size_t)r.seg_cap * n * (size_t)buf;
+    const size_t lists = (size_t)r.lists_steps * n * (size_t)buf;
+    SegBuf b;
+    b.pos = r.seg_pos + states;
+    b.vel = r.seg_vel + states;
+    b.cnt = r.seg_cnt + states;
+    b.sorted = r.seg_sorted ? r.seg_sorted + lists : nullptr;
+    b.keys = r.seg_keys ? r.seg_keys + lists : nullptr;
+    b.vals = r.seg_vals ? r.seg_vals + lists : nullptr;
+    b.off = r.seg_off ? r.seg_off + r.lists_cells * (size_t)r.lists_steps * (size_t)buf : nullptr;
+    return b;
+}
+
+// Replay of segment `seg` from its checkpoint on the world's stream, keeping
+// every state in buffer `buf` and, with lists, every step's cell list.
+int replay_segment(cf_world* w, const StepConsts& c, int seg, const SegBuf& b, bool lists)
 {
     Rollout& r = w->ro;
     const size_t n = (size_t)w->n;
+    const int len = std::min(r.every, r.steps - seg * r.every);
+    Scratch& s = w->s;
+    int rc = copy_state(w, w->pos, w->vel, w->counts, r.ckpt_pos + n * seg, r.ckpt_vel + n * seg,
+                        r.ckpt_cnt + n * seg);
+    if (rc) return rc;
+    for (int t = 0; t < len; t++) {
+        rc = copy_state(w, b.pos + n * t, b.vel + n * t, b.cnt + n * t, w->pos, w->vel, w->counts);
+        if (rc) return rc;
+        if (lists) {
+            // the replayed step builds its cell list straight into step t's arrays
+            // (the tiled build leaves it in keys[1] / vals[1]), kept for the adjoint step
+            float4* const ps = s.pos_sorted;
+            uint32_t* const k1 = s.keys[1];
+            uint32_t* const v1 = s.vals[1];
+            uint32_t* const off = s.cell_off;
+            s.pos_sorted = b.sorted + n * t;
+            s.keys[1] = b.keys + n * t;
+            s.vals[1] = b.vals + n * t;
+            s.cell_off = b.off + r.lists_cells * t;
+            rc = enqueue_step(w, c, 0);
+            s.pos_sorted = ps;
+            s.keys[1] = k1;
+            s.vals[1] = v1;
+            s.cell_off = off;
+        } else {
+            rc = enqueue_step(w, c, 0);
+        }
+        if (rc) return rc;
+    }
+    CF_CUDA(cudaMemcpyAsync(b.cnt + n * len, w->counts, sizeof(int) * n, cudaMemcpyDeviceToDevice, w->stream));
+    return CF_OK;
+}
+
+// The adjoint steps of segment `seg` in reverse, from buffer `buf`.
+int adjoint_segment(cf_world* w, const StepConsts& c, int seg, const SegBuf& b, bool lists)
+{
+    Rollout& r = w->ro;
+    const size_t n = (size_t)w->n;
+    const int len = std::min(r.every, r.steps - seg * r.every);
+    Scratch& s = w->s;
+    for (int t = len - 1; t >= 0; t--) {
+        if (lists) {
+            CF_CUDA(launch_adjoint_step(c, w->tables, b.sorted + n * t, b.keys + n * t, b.vals + n * t,
+                                        b.off + r.lists_cells * t, b.vel + n * t, b.cnt + n * t,
+                                        b.cnt + n * (t + 1), r.gx, r.gv, r.gf_sorted, r.ga_sorted, r.gacc,
+                                        w->stream));
+            continue;
+        }
+        int which = 0;
+        CF_CUDA(launch_cell_list_csr(b.pos + n * t, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, nullptr,
+                                     nullptr, w->err, &which, w->stream));
+        CF_CUDA(launch_adjoint_step(c, w->tables, s.pos_sorted, s.keys[which], s.vals[which], s.cell_off,
+                                    b.vel + n * t, b.cnt + n * t, b.cnt + n * (t + 1), r.gx, r.gv, r.gf_sorted,
+                                    r.ga_sorted, r.gacc, w->stream));
+    }
+    return CF_OK;
+}
+
+// The whole backward: save the final state, then per segment (last first)
+// replay the forward from its checkpoint keeping every state, and run the
+// adjoint steps of the segment in reverse; restore the final state.  gx / gv
+// hold dL/dx_K and dL/dv_K on entry, dL/dx_0 and dL/dv_0 on exit.  With
+// `overlap` (while capturing the backward's graph, per-step cell lists kept),
+// the replay of segment s - 1 runs on the side stream while the adjoint steps
+// of segment s run on the world's stream: the replay touches the world state,
+// the cell-list scratch and segment buffer (s - 1) & 1 only, the adjoint steps
+// buffer s & 1 and the gradients only; the replay forks after the adjoint
+// steps of segment s + 1 (which read the same buffer) and joins before those
+// of segment s - 1.
+int enqueue_rollout_backward(cf_world* w, const StepConsts& c, bool overlap)
+{
+    Rollout& r = w->ro;
     int rc = copy_state(w, r.fin_pos, r.fin_vel, r.fin_cnt, w->pos, w->vel, w->counts);
     if (rc) return rc;
     CF_CUDA(cudaMemsetAsync(r.gacc, 0, sizeof(double) * kGradAccEntries, w->stream));
     const int segs = (r.steps + r.every - 1) / r.every;
-    Scratch& s = w->s;
     // keep the replay's cell lists when the tiled build is used (it always leaves the
     // sorted keys and indices in buffer 1) and the lists are allocated for this grid
     const bool lists = cell_list_tiles(c.grid) > 0 && r.seg_off && r.lists_steps >= std::min(r.every, r.steps) &&
                        r.lists_cells >= (size_t)c.grid.cells + 1;
+    const size_t n = (size_t)w->n;
+    if (!(overlap && lists && segs > 1 && r.side)) {
+        const SegBuf b = seg_buf(r, n, 0);
+        for (int seg = segs - 1; seg >= 0; seg--) {
+            rc = replay_segment(w, c, seg, b, lists);
+            if (!rc) rc = adjoint_segment(w, c, seg, b, lists);
+            if (rc) return rc;
+        }
+        return copy_state(w, w->pos, w->vel, w->counts, r.fin_pos, r.fin_vel, r.fin_cnt);
+    }
+    const cudaStream_t own = w->stream;
+    rc = replay_segment(w, c, segs - 1, seg_buf(r, n, (segs - 1) & 1), lists);
+    if (rc) return rc;
     for (int seg = segs - 1; seg >= 0; seg--) {
-        const int s0 = seg * r.every;
-        const int len = std::min(r.every, r.steps - s0);
-        rc = copy_state(w, w->pos, w->vel, w->counts, r.ckpt_pos + n * seg, r.ckpt_vel + n * seg,
-                        r.ckpt_cnt + n * seg);
+        if (seg > 0) {
+            CF_CUDA(cudaEventRecord(r.ev_fork, own));
+            CF_CUDA(cudaStreamWaitEvent(r.side, r.ev_fork, 0));
+            w->stream = r.side;
+            rc = replay_segment(w, c, seg - 1, seg_buf(r, n, (seg - 1) & 1), lists);
+            w->stream = own;
+            if (rc) return rc;
+            CF_CUDA(cudaEventRecord(r.ev_join, r.side));
+        }
+        rc = adjoint_segment(w, c, seg, seg_buf(r, n, seg & 1), lists);
         if (rc) return rc;
-        for (int t = 0; t < len; t++) {
-            rc = copy_state(w, r.seg_pos + n * t, r.seg_vel + n * t, r.seg_cnt + n * t, w->pos, w->vel, w->counts);
-            if (rc) return rc;
-            if (lists) {
-                // the replayed step builds its cell list straight into step t's arrays
-                // (the tiled build leaves it in keys[1] / vals[1]), kept for the adjoint step
-                float4* const ps = s.pos_sorted;
-                uint32_t* const k1 = s.keys[1];
-                uint32_t* const v1 = s.vals[1];
-                uint32_t* const off = s.cell_off;
-                s.pos_sorted = r.seg_sorted + n * t;
-                s.keys[1] = r.seg_keys + n * t;
-                s.vals[1] = r.seg_vals + n * t;
-                s.cell_off = r.seg_off + r.lists_cells * t;
-                rc = enqueue_step(w, c, 0);
-                s.pos_sorted = ps;
-                s.keys[1] = k1;
-                s.vals[1] = v1;
-                s.cell_off = off;
-            } else {
-                rc = enqueue_step(w, c, 0);
-            }
-            if (rc) return rc;
-        }
-        CF_CUDA(cudaMemcpyAsync(r.seg_cnt + n * len, w->counts, sizeof(int) * n, cudaMemcpyDeviceToDevice,
-                                w->stream));
-        for (int t = len - 1; t >= 0; t--) {
-            if (lists) {
-                CF_CUDA(launch_adjoint_step(c, w->tables, r.seg_sorted + n * t, r.seg_keys + n * t,
-                                            r.seg_vals + n * t, r.seg_off + r.lists_cells * t, r.seg_vel + n * t,
-                                            r.seg_cnt + n * t, r.seg_cnt + n * (t + 1), r.gx, r.gv, r.gf_sorted,
-                                            r.ga_sorted, r.gacc, w->stream));
-                continue;
-            }
-            int which = 0;
-            CF_CUDA(launch_cell_list_csr(r.seg_pos + n * t, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, nullptr,
-                                         nullptr, w->err, &which, w->stream));
-            CF_CUDA(launch_adjoint_step(c, w->tables, s.pos_sorted, s.keys[which], s.vals[which], s.cell_off,
-                                        r.seg_vel + n * t, r.seg_cnt + n * t, r.seg_cnt + n * (t + 1), r.gx, r.gv,
-                                        r.gf_sorted, r.ga_sorted, r.gacc, w->stream));
-        }
+        if (seg > 0) CF_CUDA(cudaStreamWaitEvent(own, r.ev_join, 0));
     }
     return copy_state(w, w->pos, w->vel, w->counts, r.fin_pos, r.fin_vel, r.fin_cnt);
 }
@@ -2104,8 +2181,13 @@ int cf_rollout_backward(cf_world* w, const float* d_gpos4, const float* d_gvel4,
             if (r.bwd_graph) cudaGraphExecDestroy(r.bwd_graph);
             r.bwd_graph = nullptr;
             cudaGraph_t graph = nullptr;
+            if (!r.side) {
+                CF_CUDA(cudaStreamCreateWithFlags(&r.side, cudaStreamNonBlocking));
+                CF_CUDA(cudaEventCreateWithFlags(&r.ev_fork, cudaEventDisableTiming));
+                CF_CUDA(cudaEventCreateWithFlags(&r.ev_join, cudaEventDisableTiming));
+            }
             CF_CUDA(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
-            rc = enqueue_rollout_backward(w, c);
+            rc = enqueue_rollout_backward(w, c, true);
             cudaError_t e = cudaStreamEndCapture(w->stream, &graph);
             if (rc) {
                 if (graph) cudaGraphDestroy(graph);
@@ -2125,7 +2207,7 @@ int cf_rollout_backward(cf_world* w, const float* d_gpos4, const float* d_gvel4,
         CF_CUDA(cudaGraphLaunch(r.bwd_graph, w->stream));
         note_launches(w->stream, r.bwd_kernels);
     } else {
-        rc = enqueue_rollout_backward(w, c);
+        rc = enqueue_rollout_backward(w, c, false);
         if (rc) return rc;
     }
     if (d_gpos4_out)

@@ -140,7 +140,7 @@ constexpr int kForceStages = 4;
 struct Rollout {
     int n_cap = 0;     // particles the buffers hold
     int ckpt_cap = 0;  // checkpoint states allocated
-    int seg_cap = 0;   // segment states allocated (checkpoint_every + 1)
+    int seg_cap = 0;   // segment states per segment buffer (checkpoint_every + 1); two buffers
     float4* ckpt_pos = nullptr;
     float4* ckpt_vel = nullptr;
     int* ckpt_cnt = nullptr;
@@ -156,7 +156,7 @@ struct Rollout {
     uint32_t* seg_keys = nullptr;
     uint32_t* seg_vals = nullptr;
     uint32_t* seg_off = nullptr;
-    int lists_steps = 0;   // steps the lists hold
+    int lists_steps = 0;   // steps the lists hold, per segment buffer (two buffers)
     size_t lists_cells = 0;  // cells + 1 per step's offsets
     float4* gx = nullptr;         // dL/dx of the current step boundary
     float4* gv = nullptr;         // dL/dv
@@ -170,6 +170,11 @@ struct Rollout {
     cf_step_params params{};
     uint64_t table_version = 0;
     float radio[CF_MAX_TYPES] = {};
+    // a second stream and fork/join events: while the adjoint steps of segment s
+    // run on the world's stream, the replay of segment s - 1 runs on this one
+    // (captured into the backward's graph); segment buffers alternate by parity
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // the backward as one CUDA graph, re-captured when its key changes
     cudaGraphExec_t bwd_graph = nullptr;
     long long bwd_kernels = 0;  // kernel nodes of bwd_graph
