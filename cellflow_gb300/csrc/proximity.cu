@@ -121,6 +121,125 @@ __global__ void __launch_bounds__(kThreads)
     count[i] = (uint32_t)emit;
 }
 
+// The CSR cell list's selection with one warp per particle (grid-stride): the
+// warp stages the particle's clipped stencil (at most nine rows, one contiguous
+// range each, one lane per row, concatenated by a prefix sum) as a list of
+// sorted slots and its lanes test 32 candidates at a time.  Qualifying
+// candidates join the held set one at a time in ballot order; the set lives in
+// lanes 0 .. held-1, ordered by index, and keeps the 2*maxConn smallest indices,
+// as the per-thread kernel does.  The final order is the stable sort by squared
+// distance of that index-ordered set, i.e. by (distance, index): each held lane
+// counts the entries before it.
+constexpr int kSelWarps = kThreads / 32;
+constexpr int kSelListCap = 256;
+
+__global__ void __launch_bounds__(kThreads)
+    proximity_select_warp_kernel(const float4* __restrict__ pos_sorted, const uint32_t* __restrict__ keys_sorted,
+                                 const uint32_t* __restrict__ vals_sorted, const uint32_t* __restrict__ cell_off,
+                                 Grid g, int n, float dsq, int max_conn, int32_t* __restrict__ slots,
+                                 uint32_t* __restrict__ count)
+{
+    __shared__ uint32_t s_list[kSelWarps][kSelListCap];
+    const int lane = threadIdx.x & 31;
+    uint32_t* list = s_list[threadIdx.x >> 5];
+    const int warps = (int)gridDim.x * kSelWarps;
+    const int mx = g.m[0], my = g.m[1], mz = g.m[2];
+    const int cap = 2 * max_conn;
+    for (int t = (int)blockIdx.x * kSelWarps + (threadIdx.x >> 5); t < n; t += warps) {
+        const float4 h = pos_sorted[t];
+        const uint32_t i = vals_sorted[t];
+        if (cap <= 0) {
+            if (lane == 0) count[i] = 0;
+            continue;
+        }
+        const uint32_t key = keys_sorted[t];
+        const int cx = (int)(key % (uint32_t)mx);
+        const int cy = (int)((key / (uint32_t)mx) % (uint32_t)my);
+        const int cz = (int)(key / (uint32_t)(mx * my));
+        const int xlo = max(cx - 1, 0), xhi = min(cx + 1, mx - 1);
+        const int ylo = max(cy - 1, 0), yhi = min(cy + 1, my - 1);
+        const int zlo = max(cz - 1, 0), zhi = min(cz + 1, mz - 1);
+        const int ny = yhi - ylo + 1, nrows = ny * (zhi - zlo + 1);
+        uint32_t beg = 0u;
+        int len = 0;
+        if (lane < nrows) {
+            const int y = ylo + lane % ny, z = zlo + lane / ny;
+            const uint32_t row = (uint32_t)((z * my + y) * mx);
+            beg = cell_off[row + xlo];
+            len = (int)(cell_off[row + xhi + 1] - beg);
+        }
+        int incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int pre = incl - len;
+        int held = 0;
+        int hj = 0;
+        float hd = 0.0f;
+        for (int base = 0; base < total; base += kSelListCap) {
+            const int j0 = max(0, base - pre), j1 = min(len, base + kSelListCap - pre);
+            for (int j = j0; j < j1; j++) list[pre + j - base] = beg + (uint32_t)j;
+            __syncwarp();
+            const int lim = min(kSelListCap, total - base);
+            for (int g0 = 0; g0 < lim; g0 += 32) {
+                const int gg = g0 + lane;
+                bool ok = false;
+                int cj = 0;
+                float cd = 0.0f;
+                if (gg < lim) {
+                    const uint32_t u = list[gg];
+                    const float4 q = pos_sorted[u];
+                    if (__float_as_uint(q.w) == __float_as_uint(h.w)) {
+                        cj = (int)vals_sorted[u];
+                        if (cj > (int)i) {
+                            const float dx = __fsub_rn(q.x, h.x);
+                            const float dy = __fsub_rn(q.y, h.y);
+                            const float dz = __fsub_rn(q.z, h.z);
+                            cd = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                            ok = cd < dsq;
+                        }
+                    }
+                }
+                uint32_t qm = __ballot_sync(0xffffffffu, ok);
+                while (qm) {
+                    const int src = __ffs(qm) - 1;
+                    qm &= qm - 1u;
+                    const int j = __shfl_sync(0xffffffffu, cj, src);
+                    const float d2 = __shfl_sync(0xffffffffu, cd, src);
+                    // its place in the index-ordered set; past the end of a full set it is dropped
+                    const int pos = __popc(__ballot_sync(0xffffffffu, lane < held && hj < j));
+                    if (pos >= cap) continue;
+                    const int uj = __shfl_up_sync(0xffffffffu, hj, 1);
+                    const float ud = __shfl_up_sync(0xffffffffu, hd, 1);
+                    if (lane > pos && lane < cap) {
+                        hj = uj;
+                        hd = ud;
+                    }
+                    if (lane == pos) {
+                        hj = j;
+                        hd = d2;
+                    }
+                    held = min(held + 1, cap);
+                }
+            }
+            __syncwarp();
+        }
+        // stable sort by squared distance (ParticleSimulation.cu:235-243): rank by (distance, index)
+        int rank = 0;
+        for (int r = 0; r < held; r++) {
+            const float od = __shfl_sync(0xffffffffu, hd, r);
+            const int oj = __shfl_sync(0xffffffffu, hj, r);
+            rank += (od < hd || (od == hd && oj < hj)) ? 1 : 0;
+        }
+        const int emit = min(held, max_conn);
+        if (lane < held && rank < emit) slots[(size_t)i * CF_MAX_PROX_CONN + rank] = hj;
+        if (lane == 0) count[i] = (uint32_t)emit;
+    }
+}
+
 __global__ void __launch_bounds__(256)
     proximity_edges_kernel(const int32_t* __restrict__ slots, const uint32_t* __restrict__ offsets, int n,
                            int32_t* __restrict__ edges, int cap)
@@ -326,8 +445,9 @@ cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* ke
     if (n <= 0) return cudaSuccess;
     const int blocks = (n + kThreads - 1) / kThreads;
     if (csr) {
-        proximity_select_kernel<true><<<blocks, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted, cell_start,
-                                                                  cell_end, g, n, dsq, max_conn, slots, count);
+        const int warp_blocks = (n + kSelWarps - 1) / kSelWarps;
+        proximity_select_warp_kernel<<<warp_blocks, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted,
+                                                                      cell_start, g, n, dsq, max_conn, slots, count);
         note_launches(st);
     } else {
         proximity_select_kernel<false><<<blocks, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted, cell_start,
