@@ -1128,8 +1128,17 @@ int enqueue_host_step(cf_world* w, const StepConsts& c, const cf_particle* in, c
     CF_CUDA(launch_aos_to_soa(w->aos, w->pos, w->vel, w->acc, w->n, w->stream));
     int rc = enqueue_step(w, c, 0);
     if (rc) return rc;
-    CF_CUDA(launch_soa_to_aos(w->pos, w->vel, w->acc, w->aos, w->n, w->stream));
-    CF_CUDA(cudaMemcpyAsync(out, w->aos, bytes, cudaMemcpyDeviceToHost, w->stream));
+    // the records go back by a kernel writing the page-locked buffer through its
+    // device view (no staging copy); a buffer without one takes the staging path
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, out) == cudaSuccess && a.devicePointer) {
+        CF_CUDA(launch_soa_to_aos_mapped(w->pos, w->vel, w->acc, static_cast<cf_particle*>(a.devicePointer), w->n,
+                                         w->stream));
+    } else {
+        cudaGetLastError();
+        CF_CUDA(launch_soa_to_aos(w->pos, w->vel, w->acc, w->aos, w->n, w->stream));
+        CF_CUDA(cudaMemcpyAsync(out, w->aos, bytes, cudaMemcpyDeviceToHost, w->stream));
+    }
     CF_CUDA(cudaMemcpyAsync(&w->host_words[0], w->err, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
     return CF_OK;
 }

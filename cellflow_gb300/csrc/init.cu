@@ -87,7 +87,40 @@ __global__ void __launch_bounds__(kThreads)
     aos[i] = o;
 }
 
+// The same records written straight into page-locked host memory (its device
+// view), one 32-bit word per thread so that consecutive threads write
+// consecutive words of the 44-B records: the stores cross the CPU-GPU link as
+// whole lines, with no staging buffer or separate copy.
+__global__ void __launch_bounds__(kThreads)
+    soa_to_aos_words_kernel(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                            const float4* __restrict__ acc, uint32_t* __restrict__ words, int n)
+{
+    constexpr int kWords = (int)(sizeof(cf_particle) / sizeof(uint32_t));
+    const long long t = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (t >= (long long)kWords * n) return;
+    const int i = (int)(t / kWords), k = (int)(t - (long long)kWords * i);
+    uint32_t v;
+    if (k < 3) v = __float_as_uint(reinterpret_cast<const float*>(pos + i)[k]);
+    else if (k < 6) v = __float_as_uint(reinterpret_cast<const float*>(vel + i)[k - 3]);
+    else if (k < 9) v = __float_as_uint(reinterpret_cast<const float*>(acc + i)[k - 6]);
+    else if (k == 9) v = __float_as_uint(pos[i].w) & kTypeMask;  // world bits stay internal
+    else v = 0u;                                                // pad
+    words[t] = v;
+}
+
 }  // namespace
+
+cudaError_t launch_soa_to_aos_mapped(const float4* pos, const float4* vel, const float4* acc, cf_particle* aos_host,
+                                     int n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    static_assert(sizeof(cf_particle) == 11 * sizeof(uint32_t), "44-B records");
+    const long long words = 11LL * n;
+    soa_to_aos_words_kernel<<<(unsigned)((words + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+        pos, vel, acc, reinterpret_cast<uint32_t*>(aos_host), n);
+    note_launches(st);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_init_particles(float4* pos, float4* vel, float4* acc, int* counts, int n, int num_types,
                                   const float* lo, const float* span, uint64_t seed, cudaStream_t st, uint32_t world)
