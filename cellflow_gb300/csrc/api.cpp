@@ -1124,12 +1124,20 @@ bool page_locked(const void* p)
 int enqueue_host_step(cf_world* w, const StepConsts& c, const cf_particle* in, cf_particle* out)
 {
     const size_t bytes = sizeof(cf_particle) * (size_t)w->n;
-    CF_CUDA(cudaMemcpyAsync(w->aos, in, bytes, cudaMemcpyHostToDevice, w->stream));
-    CF_CUDA(launch_aos_to_soa(w->aos, w->pos, w->vel, w->acc, w->n, w->stream));
+    // records in and out by kernels reading and writing the page-locked buffers
+    // through their device views (no staging copies); a buffer without one takes
+    // the staging path
+    cudaPointerAttributes ai{};
+    if (cudaPointerGetAttributes(&ai, in) == cudaSuccess && ai.devicePointer) {
+        CF_CUDA(launch_aos_to_soa_mapped(static_cast<const cf_particle*>(ai.devicePointer), w->pos, w->vel, w->acc,
+                                         w->n, w->stream));
+    } else {
+        cudaGetLastError();
+        CF_CUDA(cudaMemcpyAsync(w->aos, in, bytes, cudaMemcpyHostToDevice, w->stream));
+        CF_CUDA(launch_aos_to_soa(w->aos, w->pos, w->vel, w->acc, w->n, w->stream));
+    }
     int rc = enqueue_step(w, c, 0);
     if (rc) return rc;
-    // the records go back by a kernel writing the page-locked buffer through its
-    // device view (no staging copy); a buffer without one takes the staging path
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, out) == cudaSuccess && a.devicePointer) {
         CF_CUDA(launch_soa_to_aos_mapped(w->pos, w->vel, w->acc, static_cast<cf_particle*>(a.devicePointer), w->n,

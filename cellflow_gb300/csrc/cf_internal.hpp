@@ -338,6 +338,8 @@ cudaError_t launch_aos_to_soa(const cf_particle* aos, float4* pos, float4* vel, 
 cudaError_t launch_soa_to_aos(const float4* pos, const float4* vel, const float4* acc, cf_particle* aos, int n,
                               cudaStream_t st);
 // aos_host: the device view of page-locked host records
+cudaError_t launch_aos_to_soa_mapped(const cf_particle* aos_host, float4* pos, float4* vel, float4* acc, int n,
+                                     cudaStream_t st);
 cudaError_t launch_soa_to_aos_mapped(const float4* pos, const float4* vel, const float4* acc, cf_particle* aos_host,
                                      int n, cudaStream_t st);
 cudaError_t launch_work_counters(const float4* pos, const int* counts, int n, const Grid& canon, uint32_t* pop,

@@ -108,7 +108,39 @@ __global__ void __launch_bounds__(kThreads)
     words[t] = v;
 }
 
+// The reverse: one word of the page-locked records per thread (consecutive
+// threads read consecutive words), scattered into the state arrays.
+__global__ void __launch_bounds__(kThreads)
+    aos_words_to_soa_kernel(const uint32_t* __restrict__ words, float4* __restrict__ pos, float4* __restrict__ vel,
+                            float4* __restrict__ acc, int n)
+{
+    constexpr int kWords = (int)(sizeof(cf_particle) / sizeof(uint32_t));
+    const long long t = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (t >= (long long)kWords * n) return;
+    const int i = (int)(t / kWords), k = (int)(t - (long long)kWords * i);
+    const uint32_t v = words[t];
+    if (k < 3) reinterpret_cast<float*>(pos + i)[k] = __uint_as_float(v);
+    else if (k < 6) reinterpret_cast<float*>(vel + i)[k - 3] = __uint_as_float(v);
+    else if (k < 9) reinterpret_cast<float*>(acc + i)[k - 6] = __uint_as_float(v);
+    else if (k == 9) pos[i].w = __uint_as_float(v);  // the type, as the per-record conversion stores it
+    else {
+        vel[i].w = 0.0f;
+        acc[i].w = 0.0f;
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_aos_to_soa_mapped(const cf_particle* aos_host, float4* pos, float4* vel, float4* acc, int n,
+                                     cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    const long long words = 11LL * n;
+    aos_words_to_soa_kernel<<<(unsigned)((words + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+        reinterpret_cast<const uint32_t*>(aos_host), pos, vel, acc, n);
+    note_launches(st);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_soa_to_aos_mapped(const float4* pos, const float4* vel, const float4* acc, cf_particle* aos_host,
                                      int n, cudaStream_t st)
