@@ -20,6 +20,7 @@
 namespace cf {
 namespace {
 
+
 thread_local std::string g_error;
 
 constexpr int kMaxCells = 1 << 22;        // cap of the step and proximity grids
@@ -874,6 +875,10 @@ int cf_initialize_particles(cf_world* w, uint64_t seed, float spawn_region)
     return sync_and_check(w);
 }
 
+namespace {
+void* device_view(const void* p);  // page-locked host memory's device view, or nullptr
+}  // namespace
+
 int cf_get_particles(cf_world* w, cf_particle* out, int n)
 {
     int rc = check_world(w);
@@ -881,6 +886,11 @@ int cf_get_particles(cf_world* w, cf_particle* out, int n)
     if (n != w->n || (!out && n > 0)) return fail(CF_ERR_INVALID, "output must hold exactly n particles");
     rc = ensure_aos(w);
     if (rc) return rc;
+    if (void* dout = n > 0 ? device_view(out) : nullptr) {
+        // page-locked: written word by word through its device view, no staging copy
+        CF_CUDA(launch_soa_to_aos_mapped(w->pos, w->vel, w->acc, static_cast<cf_particle*>(dout), n, w->stream));
+        return sync_and_check(w);
+    }
     CF_CUDA(launch_soa_to_aos(w->pos, w->vel, w->acc, w->aos, n, w->stream));
     if (n > 0)
         CF_CUDA(cudaMemcpyAsync(out, w->aos, sizeof(cf_particle) * (size_t)n, cudaMemcpyDeviceToHost, w->stream));
@@ -894,6 +904,11 @@ int cf_set_particles(cf_world* w, const cf_particle* in, int n)
     if (n != w->n || (!in && n > 0)) return fail(CF_ERR_INVALID, "input must hold exactly n particles");
     rc = ensure_aos(w);
     if (rc) return rc;
+    if (const void* din = n > 0 ? device_view(in) : nullptr) {
+        // page-locked: read word by word through its device view, no staging copy
+        CF_CUDA(launch_aos_to_soa_mapped(static_cast<const cf_particle*>(din), w->pos, w->vel, w->acc, n, w->stream));
+        return CF_OK;
+    }
     if (n > 0)
         CF_CUDA(cudaMemcpyAsync(w->aos, in, sizeof(cf_particle) * (size_t)n, cudaMemcpyHostToDevice, w->stream));
     CF_CUDA(launch_aos_to_soa(w->aos, w->pos, w->vel, w->acc, n, w->stream));
@@ -1107,6 +1122,18 @@ namespace {
 
 // Page-locked host memory (cudaHostAlloc or cudaHostRegister): copies from and
 // to it can be recorded in a CUDA graph.
+// The device view of page-locked host memory, or nullptr (pageable memory,
+// device memory, or a pointer the runtime does not know).
+void* device_view(const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 bool page_locked(const void* p)
 {
     cudaPointerAttributes a{};
@@ -1127,23 +1154,18 @@ int enqueue_host_step(cf_world* w, const StepConsts& c, const cf_particle* in, c
     // records in and out by kernels reading and writing the page-locked buffers
     // through their device views (no staging copies); a buffer without one takes
     // the staging path
-    cudaPointerAttributes ai{};
-    if (cudaPointerGetAttributes(&ai, in) == cudaSuccess && ai.devicePointer) {
-        CF_CUDA(launch_aos_to_soa_mapped(static_cast<const cf_particle*>(ai.devicePointer), w->pos, w->vel, w->acc,
-                                         w->n, w->stream));
+    if (const void* din = device_view(in)) {
+        CF_CUDA(launch_aos_to_soa_mapped(static_cast<const cf_particle*>(din), w->pos, w->vel, w->acc, w->n,
+                                         w->stream));
     } else {
-        cudaGetLastError();
         CF_CUDA(cudaMemcpyAsync(w->aos, in, bytes, cudaMemcpyHostToDevice, w->stream));
         CF_CUDA(launch_aos_to_soa(w->aos, w->pos, w->vel, w->acc, w->n, w->stream));
     }
     int rc = enqueue_step(w, c, 0);
     if (rc) return rc;
-    cudaPointerAttributes a{};
-    if (cudaPointerGetAttributes(&a, out) == cudaSuccess && a.devicePointer) {
-        CF_CUDA(launch_soa_to_aos_mapped(w->pos, w->vel, w->acc, static_cast<cf_particle*>(a.devicePointer), w->n,
-                                         w->stream));
+    if (void* dout = device_view(out)) {
+        CF_CUDA(launch_soa_to_aos_mapped(w->pos, w->vel, w->acc, static_cast<cf_particle*>(dout), w->n, w->stream));
     } else {
-        cudaGetLastError();
         CF_CUDA(launch_soa_to_aos(w->pos, w->vel, w->acc, w->aos, w->n, w->stream));
         CF_CUDA(cudaMemcpyAsync(out, w->aos, bytes, cudaMemcpyDeviceToHost, w->stream));
     }
