@@ -141,10 +141,15 @@ int cf_initialize_particles(cf_world* w, uint64_t seed, float spawn_region);
 
 /* ---- particle state ---------------------------------------------------- */
 
-/* getParticleData (ParticleSimulation.cu:558-562): AoS 44-byte records. */
+/* getParticleData (ParticleSimulation.cu:558-562): AoS 44-byte records;
+ * synchronises.  A page-locked `out` is written directly by the conversion
+ * kernel through its device view (no staging copy). */
 int cf_get_particles(cf_world* w, cf_particle* out, int n);
 /* Upload AoS records (the reference had no setter; its init kernel wrote
- * them).  Positions must lie in [0,W)x[0,H)x[0,D), types in [0,T). */
+ * them).  Positions must lie in [0,W)x[0,H)x[0,D), types in [0,T).  A
+ * page-locked `in` is read directly by the conversion kernel, later on the
+ * world's stream: keep it unchanged until the stream has passed that point
+ * (cf_sync), as with any asynchronous copy from page-locked memory. */
 int cf_set_particles(cf_world* w, const cf_particle* in, int n);
 /* Structure-of-arrays state: pos4/vel4 are float[4n] (type bits in pos4.w),
  * counts int[n] (the neighbour counts the next step reads as "previous"). */
@@ -189,8 +194,9 @@ int cf_step(cf_world* w, const cf_step_params* p, int nsteps);
  * memory: uploads the 44-B records from `in`, steps once (as cf_step), and
  * writes the records to `out`; synchronises and reports device errors.
  * Equivalent to cf_set_particles + cf_step + cf_get_particles.  When `in` and
- * `out` are page-locked (cudaHostAlloc / cudaHostRegister) the copies and
- * kernels run as one cached CUDA graph; otherwise as the three calls.  `in`
+ * `out` are page-locked (cudaHostAlloc / cudaHostRegister) the conversion
+ * kernels read and write them directly and the step runs as one cached CUDA
+ * graph; otherwise as the three calls.  `in`
  * and `out` may be the same buffer.  No counterpart in the reference (its
  * state stays on the device and only getParticleData copies it back). */
 int cf_step_host(cf_world* w, const cf_step_params* p, const cf_particle* in, cf_particle* out, int n);
