@@ -115,6 +115,7 @@ void free_rollout(cf_world* w)
 {
     Rollout& r = w->ro;
     if (r.bwd_graph) cudaGraphExecDestroy(r.bwd_graph);
+    if (r.fwd_graph) cudaGraphExecDestroy(r.fwd_graph);
     if (r.ev_fork) cudaEventDestroy(r.ev_fork);
     if (r.ev_join) cudaEventDestroy(r.ev_join);
     if (r.side) cudaStreamDestroy(r.side);
@@ -2154,23 +2155,50 @@ int cf_rollout_forward(cf_world* w, const cf_step_params* p, const float* d_pos4
     if (d_pos4_in) CF_CUDA(launch_pack_pos(reinterpret_cast<const float4*>(d_pos4_in), w->pos, w->pos, w->n, w->stream));
     if (d_vel4_in)
         CF_CUDA(cudaMemcpyAsync(w->vel, d_vel4_in, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
-    cudaGraphExec_t exec = nullptr;
+    // the step loop with its checkpoint copies
+    auto loop = [&]() -> int {
+        for (int s = 0; s < nsteps; s++) {
+            if (s % checkpoint_every == 0) {
+                const int k = s / checkpoint_every;
+                const int e = copy_state(w, r.ckpt_pos + n * k, r.ckpt_vel + n * k, r.ckpt_cnt + n * k, w->pos,
+                                         w->vel, w->counts);
+                if (e) return e;
+            }
+            const int e = enqueue_step(w, c, 0);
+            if (e) return e;
+        }
+        return CF_OK;
+    };
     if (w->use_graphs && w->stream != nullptr) {
-        rc = step_graph(w, c, 0, &exec);
-        if (rc) return rc;
-    }
-    for (int s = 0; s < nsteps; s++) {
-        if (s % checkpoint_every == 0) {
-            const int k = s / checkpoint_every;
-            rc = copy_state(w, r.ckpt_pos + n * k, r.ckpt_vel + n * k, r.ckpt_cnt + n * k, w->pos, w->vel, w->counts);
-            if (rc) return rc;
+        // one graph for the whole loop, re-captured when its shape or buffers change
+        const void* bufs = w->s.cell_start;
+        if (!(r.fwd_graph && r.fwd_steps == nsteps && r.fwd_every == checkpoint_every && r.fwd_bufs == bufs &&
+              r.fwd_ckpt == r.ckpt_pos && std::memcmp(&r.fwd_key, &c, sizeof(c)) == 0)) {
+            if (r.fwd_graph) cudaGraphExecDestroy(r.fwd_graph);
+            r.fwd_graph = nullptr;
+            cudaGraph_t graph = nullptr;
+            CF_CUDA(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+            rc = loop();
+            cudaError_t e = cudaStreamEndCapture(w->stream, &graph);
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            e = graph_kernel_count(graph, &r.fwd_kernels);
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&r.fwd_graph, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+            r.fwd_key = c;
+            r.fwd_steps = nsteps;
+            r.fwd_every = checkpoint_every;
+            r.fwd_bufs = bufs;
+            r.fwd_ckpt = r.ckpt_pos;
         }
-        if (exec) {
-            CF_CUDA(cudaGraphLaunch(exec, w->stream));
-            note_launches(w->stream, w->graph_kernels[0]);
-        } else if ((rc = enqueue_step(w, c, 0))) {
-            return rc;
-        }
+        CF_CUDA(cudaGraphLaunch(r.fwd_graph, w->stream));
+        note_launches(w->stream, r.fwd_kernels);
+    } else if ((rc = loop())) {
+        return rc;
     }
     if (d_pos4_out)
         CF_CUDA(cudaMemcpyAsync(d_pos4_out, w->pos, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));

@@ -175,6 +175,14 @@ struct Rollout {
     // (captured into the backward's graph); segment buffers alternate by parity
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the forward's step loop (checkpoint copies and steps) as one CUDA graph,
+    // re-captured when its key changes
+    cudaGraphExec_t fwd_graph = nullptr;
+    long long fwd_kernels = 0;
+    StepConsts fwd_key{};
+    int fwd_steps = 0, fwd_every = 0;
+    const void* fwd_bufs = nullptr;
+    const void* fwd_ckpt = nullptr;
     // the backward as one CUDA graph, re-captured when its key changes
     cudaGraphExec_t bwd_graph = nullptr;
     long long bwd_kernels = 0;  // kernel nodes of bwd_graph
