@@ -1,7 +1,8 @@
-"""cf_kernel_launches counts every kernel the library puts on a stream: a step launched
-directly (no stream set, so no graph) and the same step replayed from its CUDA graph add
-the same number, which is also the step's launch count in the profile record; a batch
-replay adds its graph's kernel nodes; a rollout adds one step's kernels per step."""
+"""cf_kernel_launches counts every kernel the library puts on a stream: a step replayed
+from its CUDA graph on the world's own stream or on a caller's stream adds the same number,
+which is also the step's launch count in the profile record; a batch replay adds its
+graph's kernel nodes; a rollout adds one step's kernels per step; the radial distribution,
+launched directly, adds its own kernels."""
 
 import ctypes as C
 
@@ -35,7 +36,7 @@ def test_step_launches_direct_graph_and_profile_agree(cflib):
     w = inputs.Workload("tally", n=30000, num_types=5, radius=0.1, steps=1, seed=41)
     params = w.params()
     sim = world(w)
-    # default stream: direct launches
+    # the world's own stream
     direct = delta(lib, lambda: (sim.simulate(params, 3), sim.sync()))
     assert direct > 0 and direct % 3 == 0
     # own stream: one captured graph per step, replayed
@@ -90,4 +91,22 @@ def test_rollout_forward_counts_each_step(cflib):
     K = 6
     rolled = delta(lib, lambda: (sim.rollout_forward(params, K, 3, None, None, None, None), sim.sync()))
     assert rolled == K * per_step
+    sim.close()
+
+
+def test_direct_launches_are_counted(cflib):
+    """cf_rdf launches its kernels directly: the position pack, the five cell-list kernels
+    of its grid, the histogram and its normalisation."""
+    import torch
+
+    lib = _lib.load()
+    w = inputs.Workload("tally_rdf", n=8192, num_types=4, radius=0.1, steps=1, seed=53)
+    sim = world(w)
+    T, bins = w.num_types, 16
+    hist = torch.empty((T, T, bins), dtype=torch.float32, device="cuda")
+    pos4 = torch.zeros((w.n, 4), dtype=torch.float32, device="cuda")
+    pos4[:, :3] = torch.from_numpy(w.positions()).cuda()
+    torch.cuda.synchronize()
+    n = delta(lib, lambda: (sim.rdf(bins, 0.2, hist.data_ptr(), pos4.data_ptr()), sim.sync()))
+    assert n == 1 + 5 + 2
     sim.close()
