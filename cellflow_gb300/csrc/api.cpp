@@ -70,8 +70,12 @@ void drop_graphs(cf_world* w)
     if (w->batch_graph) cudaGraphExecDestroy(w->batch_graph);
     w->batch_graph = nullptr;
     w->batch_graph_steps = 0;
+    // the rollout's graphs capture the cell-list scratch (offsets, tile
+    // totals, items) by address, so any reallocation must drop them too
     if (w->ro.bwd_graph) cudaGraphExecDestroy(w->ro.bwd_graph);
     w->ro.bwd_graph = nullptr;
+    if (w->ro.fwd_graph) cudaGraphExecDestroy(w->ro.fwd_graph);
+    w->ro.fwd_graph = nullptr;
     for (int k = 0; k < 2; k++) {
         if (w->graph[k]) cudaGraphExecDestroy(w->graph[k]);
         w->graph[k] = nullptr;
@@ -1947,6 +1951,9 @@ int ensure_rollout_lists(cf_world* w, int steps, int cells)
     const size_t offs = (size_t)cells + 1;
     if (r.seg_off && steps <= r.lists_steps && offs <= r.lists_cells) return CF_OK;
     CF_CUDA(cudaStreamSynchronize(w->stream));
+    // the backward's graph reads these lists by address: drop it with them
+    if (r.bwd_graph) cudaGraphExecDestroy(r.bwd_graph);
+    r.bwd_graph = nullptr;
     for (void* p : {(void*)r.seg_sorted, (void*)r.seg_keys, (void*)r.seg_vals, (void*)r.seg_off}) dev_free(p);
     r.seg_sorted = nullptr;
     r.seg_keys = r.seg_vals = r.seg_off = nullptr;

@@ -102,6 +102,40 @@ def test_checkpoint_interval_does_not_change_gradients(cflib):
         np.testing.assert_allclose(gp, out[0][2], rtol=1e-5)
 
 
+def test_rollout_graphs_follow_scratch_reallocation(cflib):
+    """The rollout's forward and backward run as cached CUDA graphs that read the
+    cell-list scratch by address.  Proximity calls on much finer grids grow that
+    scratch between rollouts of the same shape; the rollouts after them must not
+    replay a graph holding the freed buffers: their states and gradients equal a
+    run on the default stream, where no graph is used."""
+    n, T, K, every = 3000, 4, 6, 3
+    sim, params, *_ = make_world(n, T, 0.15, 21, 0.03)
+    ref, *_ = make_world(n, T, 0.15, 21, 0.03)
+    ref.set_stream(None)
+    start = sim.get_state()
+    gx = dev4(np.ones((n, 3), np.float32))
+
+    def rollout(s, between=None):
+        s.set_state(*start)
+        s.rollout_forward(params, K, every)
+        if between is not None:
+            s.proximity_edges(between, 3)  # offsets and tile totals reallocated for the finer grid
+        g0 = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+        gF, gp = s.rollout_backward(gx.data_ptr(), None, g0.data_ptr(), None)
+        torch.cuda.synchronize()
+        return s.get_state(), g0[:, :3].cpu().numpy(), gF, gp
+
+    first = rollout(sim)
+    sim.proximity_edges(0.02, 3)  # a 100^3 grid against the step's 13^3
+    again = rollout(sim, between=0.008)  # the 4M-cell cap, between the forward and the backward
+    want = rollout(ref)
+    for got in (first, again):
+        for x, y in zip(got[0], want[0]):
+            assert np.array_equal(x, y)
+        for g, r in zip(got[1:], want[1:]):  # table gradients sum double atomics: order may differ
+            np.testing.assert_allclose(g, r, rtol=1e-6, atol=1e-7 * np.abs(r).max())
+
+
 def test_backward_state_is_the_forward_state(cflib):
     sim, params, *_ = make_world(2000, 3, 0.2, 9, 0.05)
     sim.rollout_forward(params, 5, 2)
