@@ -155,6 +155,8 @@ _SIGNATURES = {
     "cf_set_particle_count": (C.c_int, [_W, C.c_int, C.c_uint64]),
     "cf_set_num_particle_types": (C.c_int, [_W, C.c_int, C.c_uint64]),
     "cf_initialize_particles": (C.c_int, [_W, C.c_uint64, C.c_float]),
+    "cf_set_canvas": (C.c_int, [_W, C.c_float, C.c_float, C.c_float]),
+    "cf_move_universe": (C.c_int, [_W, C.c_float, C.c_float, C.c_float]),
     "cf_get_particles": (C.c_int, [_W, C.c_void_p, C.c_int]),
     "cf_set_particles": (C.c_int, [_W, C.c_void_p, C.c_int]),
     "cf_get_state": (C.c_int, [_W, C.c_void_p, C.c_void_p, C.c_void_p]),

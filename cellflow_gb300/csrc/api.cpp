@@ -870,6 +870,32 @@ int cf_set_num_particle_types(cf_world* w, int t, uint64_t seed)
     return sync_and_check(w);
 }
 
+int cf_set_canvas(cf_world* w, float width, float height, float depth)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!finite_positive(width) || !finite_positive(height) || !finite_positive(depth))
+        return fail(CF_ERR_INVALID, "box extents must be finite and positive");
+    if (width == w->ext[0] && height == w->ext[1] && depth == w->ext[2]) return CF_OK;
+    // the cached selection graphs hold the old extents as kernel arguments
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    drop_graphs(w);
+    w->ext[0] = width;
+    w->ext[1] = height;
+    w->ext[2] = depth;
+    return CF_OK;
+}
+
+int cf_move_universe(cf_world* w, float dx, float dy, float dz)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    if (!std::isfinite(dx) || !std::isfinite(dy) || !std::isfinite(dz))
+        return fail(CF_ERR_INVALID, "the shift must be finite");
+    CF_CUDA(launch_move_particles(w->pos, w->n, dx, dy, dz, w->ext, w->stream));
+    return CF_OK;
+}
+
 int cf_initialize_particles(cf_world* w, uint64_t seed, float spawn_region)
 {
     int rc = check_world(w);

@@ -342,6 +342,7 @@ cudaError_t launch_proximity_emit_vertices(const int32_t* slots, const uint32_t*
 cudaError_t launch_init_particles(float4* pos, float4* vel, float4* acc, int* counts, int n, int num_types,
                                   const float* lo, const float* span, uint64_t seed, cudaStream_t st,
                                   uint32_t world = 0);
+cudaError_t launch_move_particles(float4* pos, int n, float dx, float dy, float dz, const float* ext, cudaStream_t st);
 cudaError_t launch_aos_to_soa(const cf_particle* aos, float4* pos, float4* vel, float4* acc, int n, cudaStream_t st);
 cudaError_t launch_soa_to_aos(const float4* pos, const float4* vel, const float4* acc, cf_particle* aos, int n,
                               cudaStream_t st);

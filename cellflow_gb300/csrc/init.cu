@@ -129,7 +129,31 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// moveParticlesKernel (cuda-native/src/ParticleSimulation.cu:169-185): every
+// position translated and wrapped as fmodf((x + dx) + W, W), in that order.
+__global__ void __launch_bounds__(kThreads)
+    move_particles_kernel(float4* __restrict__ pos, int n, float dx, float dy, float dz, float ext_x, float ext_y,
+                          float ext_z)
+{
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos[i];
+    p.x = fmodf(__fadd_rn(__fadd_rn(p.x, dx), ext_x), ext_x);
+    p.y = fmodf(__fadd_rn(__fadd_rn(p.y, dy), ext_y), ext_y);
+    p.z = fmodf(__fadd_rn(__fadd_rn(p.z, dz), ext_z), ext_z);
+    pos[i] = p;
+}
+
 }  // namespace
+
+cudaError_t launch_move_particles(float4* pos, int n, float dx, float dy, float dz, const float* ext, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    move_particles_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(pos, n, dx, dy, dz, ext[0], ext[1],
+                                                                             ext[2]);
+    note_launches(st);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_aos_to_soa_mapped(const cf_particle* aos_host, float4* pos, float4* vel, float4* acc, int n,
                                      cudaStream_t st)

@@ -104,6 +104,16 @@ class ParticleSimulation:
     def initializeParticles(self, seed: int = 1, spawn_region: float = 2000.0) -> None:
         check(self._lib.cf_initialize_particles(self._h, seed, spawn_region), "cf_initialize_particles")
 
+    def updateCanvasDimensions(self, width: float, height: float, depth: float | None = None) -> None:
+        """The box that initializeParticles spawns in and moveUniverse wraps into (depth defaults
+        to height, ParticleSimulation.cu:497-503)."""
+        depth = height if depth is None else depth
+        check(self._lib.cf_set_canvas(self._h, width, height, depth), "cf_set_canvas")
+
+    def moveUniverse(self, dx: float, dy: float, dz: float = 0.0) -> None:
+        """Translate every particle and wrap into the box (ParticleSimulation.cu:585-592)."""
+        check(self._lib.cf_move_universe(self._h, dx, dy, dz), "cf_move_universe")
+
     def set_stream(self, stream_ptr: int | None) -> None:
         check(self._lib.cf_set_stream(self._h, C.c_void_p(stream_ptr or 0)), "cf_set_stream")
 

@@ -138,6 +138,18 @@ int cf_set_num_particle_types(cf_world* w, int t, uint64_t seed);
  * the reference's time-seeded cuRAND state; the type is clamped to T-1 (the
  * reference could produce T when its uniform draw was exactly 1.0). */
 int cf_initialize_particles(cf_world* w, uint64_t seed, float spawn_region);
+/* updateCanvasDimensions / initializeParticles(W, H) (ParticleSimulation.cu:497-503,
+ * :486-489): the box that cf_initialize_particles spawns in and
+ * cf_move_universe wraps into; the step itself wraps with the extents in its
+ * cf_step_params, as the reference's kernel does (:159-161). */
+int cf_set_canvas(cf_world* w, float width, float height, float depth);
+/* moveUniverse (ParticleSimulation.cuh:50, ParticleSimulation.cu:585-592,
+ * kernel :169-185): every position becomes fmodf((p + d) + W, W) per axis.
+ * The reference wrapped with a default-constructed SimulationParams' 8000-unit
+ * canvas whatever the world's box; here the world's own box is used.  A shift
+ * below -W leaves negative coordinates, as there; the next step reports them
+ * (CF_ERR_DOMAIN).  Asynchronous on the world's stream. */
+int cf_move_universe(cf_world* w, float dx, float dy, float dz);
 
 /* ---- particle state ---------------------------------------------------- */
 
