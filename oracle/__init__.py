@@ -95,7 +95,7 @@ def lib() -> C.CDLL:
         vp, P = C.c_void_p, C.POINTER(OracleParams)
         L.cfo_step_f32.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, P, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp]
         L.cfo_step_f32.restype = None
-        L.cfo_step_f64.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, P, vp, vp, vp, vp, vp]
+        L.cfo_step_f64.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, P, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp]
         L.cfo_step_f64.restype = None
         L.cfo_force_table.argtypes = [vp, C.c_int, C.c_float, C.c_float, C.c_float, vp]
         L.cfo_force_table.restype = None
@@ -201,18 +201,20 @@ def step_f32(pos, vel, types, counts, table, radio, params, rows=None):
     return po, vo, ao, co
 
 
-def step_f64(pos, vel, types, counts, table, radio, params):
-    """FP64 step from FP32 inputs; also returns per-particle term magnitude."""
+def step_f64(pos, vel, types, counts, table, radio, params, rows=None):
+    """FP64 step from FP32 inputs; also returns per-particle term magnitude.
+    rows = (begin, end, stride) selects particles as in step_f32."""
     pos, vel = _f32(pos, (-1, 3)), _f32(vel, (-1, 3))
     n = len(pos)
     types = np.ascontiguousarray(types, dtype=np.uint32)
     counts = np.ascontiguousarray(counts, dtype=np.int32)
     table, radio = _f32(table).ravel(), _f32(radio).ravel()
+    b, e, s = rows if rows else (0, n, 1)
     po, vo, ao = (np.zeros((n, 3)) for _ in range(3))
     co = np.zeros(n, dtype=np.int32)
     mag = np.zeros(n)
     lib().cfo_step_f64(n, _p(pos), _p(vel), _p(types), _p(counts), _p(table), _p(radio),
-                       C.byref(to_oracle_params(params)), _p(po), _p(vo), _p(ao), _p(co), _p(mag))
+                       C.byref(to_oracle_params(params)), b, e, s, _p(po), _p(vo), _p(ao), _p(co), _p(mag))
     return po, vo, ao, co, mag
 
 

@@ -139,14 +139,18 @@ void cfo_step_f32(int n, const float* pos, const float* vel, const uint32_t* typ
  * term is a difference (repulsion minus attraction, which cancels near their
  * crossing) and the terms are summed, so any evaluation order or few-ulp
  * function error moves the result by a small multiple of this, not of the
- * (possibly cancelled) result.  ParticleSimulation.cu:78-165.
+ * (possibly cancelled) result.  Rows selected as in cfo_step_f32.
+ * ParticleSimulation.cu:78-165.
  */
 void cfo_step_f64(int n, const float* pos, const float* vel, const uint32_t* type, const int* cnt_in, const float* F,
-                  const float* rb, const cfo_params* p, double* pos_out, double* vel_out, double* acc_out,
-                  int* cnt_out, double* mag)
+                  const float* rb, const cfo_params* p, int i_begin, int i_end, int i_stride, double* pos_out,
+                  double* vel_out, double* acc_out, int* cnt_out, double* mag)
 {
+    if (i_stride < 1) i_stride = 1;
+    int rows = (i_end - i_begin + i_stride - 1) / i_stride;
 #pragma omp parallel for schedule(dynamic, 8)
-    for (int i = 0; i < n; i++) {
+    for (int r = 0; r < rows; r++) {
+        int i = i_begin + r * i_stride;
         double px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
         double W = p->w, H = p->h, D = p->d;
         uint32_t tp = type[i];

@@ -77,8 +77,8 @@ def test_drop_in_matches_python_binding(cflib, tmp_path):
     assert int(fields["frames"]) == steps + 2 and int(fields["mapped"]) == 0
     assert int(fields["line_vertices"]) == 2 * len(edges)
     assert int(fields["triangle_vertices"]) == 3 * len(tris)
-    first = tuple(float(v) for v in r.stdout.split()[0][len("first=("):-1].split(","))
-    assert first == tuple(float(v) for v in rec["pos"][0])
+    first = np.array([float(v) for v in r.stdout.split()[0][len("first=("):-1].split(",")], np.float32)
+    assert np.array_equal(first, rec["pos"][0])  # printed with 9 digits: exact for float32
     pos_sum = float(np.sum(rec["pos"].astype(np.float64)))
     assert abs(float(fields["pos_sum"]) - pos_sum) <= 1e-9 * max(1.0, abs(pos_sum))
     assert int(float(fields["type_sum"])) == int(rec["ptype"].sum())
