@@ -37,6 +37,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 FLUSH_BYTES = 256 << 20
+REFERENCE_BUDGET_S = 240.0  # whole reference steps when the run fits in this
 
 
 def parse_args():
@@ -45,7 +46,10 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", default="plain_n100k_t8")
+    ap.add_argument("--workload", default=None,
+                    help="one workload alone (default: the 100k headline with the 1M, batched and rollout "
+                         "workloads as nested records)")
+    ap.add_argument("--no-nested", action="store_true", help="the headline workload alone")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
@@ -290,9 +294,15 @@ def run_reference_arm(args, rank, world):
             oracle.step_f32(pos, np.zeros_like(pos), types, counts, table, radio, params, rows=rows)
         return time.perf_counter() - t0, len(range(*rows)), n
 
+    # calibrate on a small strided sample; run whole steps when the whole run (warm-up and
+    # timed steps) fits in REFERENCE_BUDGET_S seconds, else strided samples of about one
+    # second per step, whose per-step time is then an extrapolation (labelled as such)
     frac = min(1.0, 8.0 * cores / max(len(world_inputs(0)[0]), 1))
     dt, r, _ = one(0, frac)
-    if dt > 0:
+    full_step_s = dt / frac if frac > 0 else dt
+    if full_step_s * (args.warmup + args.steps) <= REFERENCE_BUDGET_S:
+        frac = 1.0
+    elif dt > 0:
         frac = min(1.0, frac / dt)
     for s in range(args.warmup):
         one(s, frac)
@@ -302,12 +312,16 @@ def run_reference_arm(args, rank, world):
         total_t += dt
         total_rows += r
     value = total_rows / total_t
-    sample = (f"per step about {total_rows // max(args.steps, 1)} particles (a {frac:.3g} strided fraction of one "
-              f"world), each against all particles of its world; {cores} OpenMP threads")
+    whole = frac >= 1.0
+    sample = (f"per step about {total_rows // max(args.steps, 1)} particles "
+              + ("(every particle of the world: whole steps)" if whole else
+                 f"(a {frac:.3g} strided fraction of one world; ms_per_step extrapolated from it)")
+              + f", each against all particles of its world; {cores} OpenMP threads")
     line = {
         "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * full_n / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": 1e3 * full_n / value, "ms_per_step_measured": whole,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded Philox), see config",
         "config": config,
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": kind,
@@ -325,7 +339,10 @@ def workload_config(w) -> dict:
             "l2": "flushed between timed steps (256 MiB write)", "seed": w.seed}
 
 
-def run_gb300(args, rank, world, local):
+def run_gb300(args, rank, world, local, name, steps, warmup, cpu_seconds, extras=True):
+    """One plain-step workload: the timed steps, the force-kernel and cell-list rooflines, the CPU
+    baseline, end to end through the C ABI, and (extras) the reference kernel built for this GPU and
+    the proximity graph.  Returns rank 0's record (None on other ranks)."""
     import numpy as np
     import torch
 
@@ -333,13 +350,8 @@ def run_gb300(args, rank, world, local):
     from cellflow_gb300 import _lib, inputs
     from cellflow_gb300.world import PARTICLE_DTYPE, ParticleSimulation
 
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     lib = _lib.load()
-    w = inputs.WORKLOADS[args.workload]
+    w = inputs.WORKLOADS[name]
     params = w.params()
     pos, types, table = w.positions(), w.types(), w.table()
     radio = np.zeros(w.num_types, np.float32)
@@ -357,7 +369,7 @@ def run_gb300(args, rank, world, local):
             torch.distributed.barrier()
 
     force_variant = sim.autotune(params, 5)  # picks the force-kernel variant; restores the state
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         sim.simulate(params, 1)
     sim.sync()
     state0 = sim.get_state()
@@ -371,7 +383,7 @@ def run_gb300(args, rank, world, local):
     tally0 = lib.cf_kernel_launches()
     wall0 = time.perf_counter()
     with torch.cuda.stream(stream):
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()
             sim.simulate(params, 1)
     barrier()
@@ -383,18 +395,18 @@ def run_gb300(args, rank, world, local):
     _lib.check(lib.cf_profile_enable(sim.handle, 0), "cf_profile_enable")
     step_ms_total = prof.cell_list_ms + prof.force_ms
     t_max = max_over_ranks(step_ms_total)
-    value = replica_throughput(w.n * args.steps, t_max, world)
+    value = replica_throughput(w.n * steps, t_max, world)
 
     # ---- work counters: replay the same K steps from the same state, untimed
     sim.set_state(*state0)
     c27_total, inter_total = 0, 0
-    for _ in range(args.steps):
+    for _ in range(steps):
         c27, _ = sim.work_counters(params)
         sim.simulate(params, 1)
         _, inter = sim.work_counters(params)
         c27_total += c27
         inter_total += inter
-    flops = 9 * c27_total + 17 * inter_total + 25 * w.n * args.steps
+    flops = 9 * c27_total + 17 * inter_total + 25 * w.n * steps
     force_s = prof.force_ms * 1e-3
     achieved_tflops = flops / force_s / 1e12
     peak_fp32 = C.c_double()
@@ -403,12 +415,12 @@ def run_gb300(args, rank, world, local):
     g = sim.grid(params)
     for a in range(3):
         cells *= g.cells[a]
-    cell_bytes = (112 * w.n + 8 * cells) * args.steps
+    cell_bytes = (112 * w.n + 8 * cells) * steps
     cell_gbs = cell_bytes / (prof.cell_list_ms * 1e-3) / 1e9
     peaks = measured_peaks()
 
     # ---- end to end through the C ABI with host buffers
-    e2e_steps = args.e2e_steps or max(10, args.steps // 2)
+    e2e_steps = args.e2e_steps or max(10, steps // 2)
     host = torch.empty(w.n * PARTICLE_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
     host_np = host.numpy().view(PARTICLE_DTYPE)
     sim.set_state(*state0)
@@ -449,24 +461,25 @@ def run_gb300(args, rank, world, local):
     e2e_value = w.n * e2e_steps * world / e2e_wall
 
     # ---- reference kernel on this GPU (its O(N^2) kernel built for sm_103a), a few steps
-    ref_gpu = reference_gpu_kernel(w, params, pos, types, table, radio, stream) if rank == 0 else None
+    ref_gpu = reference_gpu_kernel(w, params, pos, types, table, radio, stream) if rank == 0 and extras else None
 
     # ---- proximity graph (edges/s) on the state the timed steps left
-    prox = proximity_timing(sim, w, stream, args.prox_calls) if w.prox_distance is not None else None
+    prox = proximity_timing(sim, w, stream, args.prox_calls) if w.prox_distance is not None and extras else None
 
     line = None
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            v, kind, cores, desc = cpu_reference_sample(w, params, pos, types, table, radio, args.cpu_seconds)
+            v, kind, cores, desc = cpu_reference_sample(w, params, pos, types, table, radio, cpu_seconds)
             cpu = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": kind, "sample": desc,
                    "cpu_model": host_cpu_model()}
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+            "steps": steps, "warmup": warmup, "ms_per_step": t_max / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Philox4x32-10), shapes and distributions of the workload",
-            "config": dict(workload_config(w), force_variant=force_variant),
+            "config": workload_config(w),
+            "force_variant": force_variant,
             "roofline": {
                 "kernel": "step_force_kernel (force + density + integrator)", "bound": "fp32",
                 "achieved": achieved_tflops, "peak": peak_fp32.value, "unit": "TFLOP/s",
@@ -474,8 +487,8 @@ def run_gb300(args, rank, world, local):
                 "peak_source": "FP32 FMA chains on every SM, measured in this run (cf_measure_fp32_peak); "
                                "MEASURED_PEAKS.json has no FP32 figure",
                 "work_model": "9*C27 + 17*I + 25*N flops per step",
-                "c27_per_particle_step": c27_total / (w.n * args.steps),
-                "interacting_per_particle_step": inter_total / (w.n * args.steps),
+                "c27_per_particle_step": c27_total / (w.n * steps),
+                "interacting_per_particle_step": inter_total / (w.n * steps),
                 "traffic": (profiled_traffic(w.name) or {}).get("bytes_per_launch"),
                 "traffic_unit": "bytes per launch (one ncu capture of this workload's force kernel)",
                 "traffic_source": (profiled_traffic(w.name) or {}).get("source"),
@@ -488,7 +501,7 @@ def run_gb300(args, rank, world, local):
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if not peaks.get("fallback") else "fallback",
                 "work_model": "112 B/particle + 8 B/cell per step",
             },
-            "phase_ms_per_step": {"cell_list": prof.cell_list_ms / args.steps, "force": prof.force_ms / args.steps},
+            "phase_ms_per_step": {"cell_list": prof.cell_list_ms / steps, "force": prof.force_ms / steps},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": w.n * 44,
                     "d2h_bytes_per_step": w.n * 44, "steps": e2e_steps,
                     "path": "cf_step_host: pinned 44-B AoS records up, one step, records back (one CUDA graph)",
@@ -503,31 +516,27 @@ def run_gb300(args, rank, world, local):
             "proximity": prox,
             "library": cf.__name__ + ": " + _lib.load().cf_version().decode(),
         }
-        print(json.dumps(line), flush=True)
+        if not extras:
+            for k in ("reference_gpu_kernel", "proximity", "library"):
+                line.pop(k)
     sim.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    return line
 
 
-def run_batched(args, rank, world, local):
-    """--workload batched_256w: 256 independent worlds stepped together (cf_batch_*), a
-    100-step loop captured in one CUDA graph and replayed; the same worlds stepped one by
-    one through the plain API (each world's step its own CUDA graph) are timed beside it.
-    One bench step is one simulation step of every world; K is rounded up to whole
-    replays of the 100-step graph."""
+def run_batched(args, rank, world, local, name="batched_256w", steps=100, warmup=100, cpu_seconds=12.0):
+    """batched_256w: 256 independent worlds stepped together (cf_batch_*), a 100-step loop
+    captured in one CUDA graph and replayed; the same worlds stepped one by one through the
+    plain API (each world's step its own CUDA graph) are timed beside it.  One bench step is
+    one simulation step of every world; K is rounded up to whole replays of the 100-step
+    graph.  The force-kernel roofline comes from profiled steps of the batch (per-phase
+    events) and the work counters of the same steps.  Returns rank 0's record."""
     import numpy as np
     import torch
 
-    import cellflow_gb300 as cf
     from cellflow_gb300 import _lib, inputs
     from cellflow_gb300.world import Batch, ParticleSimulation
 
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    bw = inputs.BATCHED[args.workload]
+    bw = inputs.BATCHED[name]
     params = bw.params()
     sizes = bw.sizes()
     parts = [bw.world(k, int(n)) for k, n in enumerate(sizes)]
@@ -537,6 +546,7 @@ def run_batched(args, rank, world, local):
     total = int(sizes.sum())
     stream = torch.cuda.Stream()
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    lib = _lib.load()
 
     def barrier():
         torch.cuda.synchronize()
@@ -550,8 +560,8 @@ def run_batched(args, rank, world, local):
     variant = batch.autotune(params, 5)
     batch.capture(params, bw.graph_steps)
     _, graph_kernels = batch.graph_info()
-    replays = max(1, -(-args.steps // bw.graph_steps))
-    warm = max(1, -(-args.warmup // bw.graph_steps))
+    replays = max(1, -(-steps // bw.graph_steps))
+    warm = max(1, -(-warmup // bw.graph_steps))
     for _ in range(warm):
         batch.replay()
     batch.sync()
@@ -560,7 +570,7 @@ def run_batched(args, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
-    tally0 = _lib.load().cf_kernel_launches()
+    tally0 = lib.cf_kernel_launches()
     with torch.cuda.stream(stream):
         for e0, e1 in ev:
             flush.zero_()
@@ -568,18 +578,45 @@ def run_batched(args, rank, world, local):
             batch.replay()
             e1.record(stream)
     barrier()
-    launches = _lib.load().cf_kernel_launches() - tally0
+    launches = lib.cf_kernel_launches() - tally0
     clk = clocks.stop()
     batch_ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
     t_max = max_over_ranks(batch_ms)
     steps_timed = replays * bw.graph_steps
     value = replica_throughput(total * steps_timed, t_max, world)
 
+    # ---- force-kernel roofline: profiled steps of the batch from the initial state (phase
+    # events), then the work counters of the same steps replayed untimed
+    wh = batch.world_handle()
+    prof_steps = min(20, bw.graph_steps)
+    batch.set_particles(pos, types)
+    _lib.check(lib.cf_profile_enable(wh, 1), "cf_profile_enable")
+    with torch.cuda.stream(stream):
+        for _ in range(prof_steps):
+            flush.zero_()
+            batch.simulate(params, 1)
+    prof = _lib.PhaseTimes()
+    _lib.check(lib.cf_profile_read(wh, C.byref(prof)), "cf_profile_read")
+    _lib.check(lib.cf_profile_enable(wh, 0), "cf_profile_enable")
+    batch.set_particles(pos, types)
+    c27_total, inter_total = 0, 0
+    pc = params.to_c()
+    for _ in range(prof_steps):
+        c27, inter = C.c_uint64(), C.c_uint64()
+        _lib.check(lib.cf_work_counters(wh, C.byref(pc), C.byref(c27), None), "cf_work_counters")
+        batch.simulate(params, 1)
+        _lib.check(lib.cf_work_counters(wh, C.byref(pc), None, C.byref(inter)), "cf_work_counters")
+        c27_total += c27.value
+        inter_total += inter.value
+    flops = 9 * c27_total + 17 * inter_total + 25 * total * prof_steps
+    achieved = flops / (prof.force_ms * 1e-3) / 1e12
+    peak_fp32 = C.c_double()
+    _lib.check(lib.cf_measure_fp32_peak(C.byref(peak_fp32)), "cf_measure_fp32_peak")
+
     # ---- end to end: host state in (pinned), one replay, host state out
     pin = lambda shape, dt: torch.empty(shape, dtype=dt).pin_memory()  # noqa: E731
     hpos, hvel, hcnt = pin((total, 4), torch.float32), pin((total, 4), torch.float32), pin((total,), torch.int32)
     batch.set_particles(pos, types)
-    lib = _lib.load()
     ptrs = [C.c_void_p(x.data_ptr()) for x in (hpos, hvel, hcnt)]
     _lib.check(lib.cf_batch_get_state(batch.handle, *ptrs), "cf_batch_get_state")
     e2e_reps = max(1, replays)
@@ -626,53 +663,106 @@ def run_batched(args, rank, world, local):
     for s in sims:
         s.close()
 
-    if rank == 0:
-        line = {
-            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
-            "steps": steps_timed, "warmup": warm * bw.graph_steps, "ms_per_step": t_max / steps_timed,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded Philox4x32-10): per world uniform positions, uniform types, N(0,0.5) table",
-            "config": {"workload": bw.name, "worlds": bw.worlds, "n_per_world": f"log-uniform [{bw.n_min}, "
-                       f"{bw.n_max}]", "total_particles": total, "n_min": int(sizes.min()),
-                       "n_max": int(sizes.max()), "types": bw.num_types, "radius": bw.radius, "dt": bw.delta_t,
-                       "graph_steps": bw.graph_steps, "replays": replays, "force_variant": variant,
-                       "l2": "flushed between replays (256 MiB write); state larger than L2", "seed": bw.seed},
-            "world_by_world": {"value": wbw_value, "unit": "particle-steps/s", "steps": wbw_steps,
-                               "path": "256 ParticleSimulation objects on one stream, one step graph each"},
-            "batched_over_world_by_world": value / wbw_value,
-            "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": total * 36 //
-                    bw.graph_steps, "d2h_bytes_per_step": total * 36 // bw.graph_steps,
-                    "path": "cf_batch_set_state (pinned) + 100-step graph replay + cf_batch_get_state",
-                    "replays": e2e_reps},
-            "gpu_launches": int(launches), "gpu_launches_expected": graph_kernels * replays,
-            "clocks": clk,
-            "library": cf.__name__ + ": " + lib.cf_version().decode(),
-        }
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return None
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = batched_cpu_sample(bw, params, sizes, parts, cpu_seconds)
+    return {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": steps_timed, "warmup": warm * bw.graph_steps, "ms_per_step": t_max / steps_timed,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Philox4x32-10): per world uniform positions, uniform types, N(0,0.5) table",
+        "config": {"workload": bw.name, "worlds": bw.worlds, "n_per_world": f"log-uniform [{bw.n_min}, "
+                   f"{bw.n_max}]", "total_particles": total, "n_min": int(sizes.min()),
+                   "n_max": int(sizes.max()), "types": bw.num_types, "radius": bw.radius, "dt": bw.delta_t,
+                   "graph_steps": bw.graph_steps, "replays": replays,
+                   "l2": "flushed between replays (256 MiB write); state larger than L2", "seed": bw.seed},
+        "force_variant": variant,
+        "world_by_world": {"value": wbw_value, "unit": "particle-steps/s", "steps": wbw_steps,
+                           "path": "256 ParticleSimulation objects on one stream, one step graph each"},
+        "batched_over_world_by_world": value / wbw_value,
+        "roofline": {
+            "kernel": "step_force_kernel (force + density + integrator), all 256 worlds in one launch",
+            "bound": "fp32", "achieved": achieved, "peak": peak_fp32.value, "unit": "TFLOP/s",
+            "frac": achieved / peak_fp32.value,
+            "peak_source": "FP32 FMA chains on every SM, measured in this run (cf_measure_fp32_peak)",
+            "work_model": "9*C27 + 17*I + 25*N flops per step",
+            "steps": prof_steps, "force_ms_per_step": prof.force_ms / max(prof.steps, 1),
+            "cell_list_ms_per_step": prof.cell_list_ms / max(prof.steps, 1),
+            "c27_per_particle_step": c27_total / (total * prof_steps),
+            "interacting_per_particle_step": inter_total / (total * prof_steps),
+        },
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": total * 36 //
+                bw.graph_steps, "d2h_bytes_per_step": total * 36 // bw.graph_steps,
+                "path": "cf_batch_set_state (pinned) + 100-step graph replay + cf_batch_get_state",
+                "replays": e2e_reps},
+        "gpu_launches": int(launches), "gpu_launches_expected": graph_kernels * replays,
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+
+
+def batched_cpu_sample(bw, params, sizes, parts, budget_s: float):
+    """The reference step on the host, world by world (it has no batching): strided rows of
+    worlds taken in a fixed order until the time budget is spent.  Returns the cpu_baseline
+    record in particle-steps/s over all the particles the sample covered."""
+    import numpy as np
+
+    import oracle
+
+    try:
+        oracle.build_ref(gpu=False)
+    except Exception:
+        pass
+    kind = "reference" if oracle.ref_available() else "port"
+    cores = os.cpu_count() or 1
+    radio = np.zeros(bw.num_types, np.float32)
+    rows_done, t_total, worlds_done = 0, 0.0, 0
+    for s in range(bw.worlds):
+        k = (37 * s) % bw.worlds
+        pos, types, table = parts[k]
+        n = len(pos)
+        stride = max(1, n // (64 * cores))
+        rows = (0, n, stride)
+        counts = np.zeros(n, np.int32)
+        t0 = time.perf_counter()
+        if kind == "reference":
+            oracle.ref_step(oracle.to_records(pos, np.zeros_like(pos), types), table, radio, counts, params, rows=rows)
+        else:
+            oracle.step_f32(pos, np.zeros_like(pos), types, counts, table, radio, params, rows=rows)
+        t_total += time.perf_counter() - t0
+        rows_done += len(range(*rows))
+        worlds_done += 1
+        if t_total > budget_s:
+            break
+    return {"value": rows_done / t_total, "unit": "particle-steps/s", "cores": cores, "kind": kind,
+            "cpu_model": host_cpu_model(),
+            "sample": f"{rows_done} particles of {worlds_done} worlds (strided rows, each against all particles "
+                      f"of its world), one step from the initial state, world by world; {cores} OpenMP threads; "
+                      f"{t_total:.2f} s"}
 
 
 ROLLOUT = {"rollout_n16k_k64": dict(n=16384, types=6, radius=0.1, steps=64, every=16, bins=32, r_max=0.2,
                                     seed=0x5EED0005)}
 
 
-def run_rollout(args, rank, world, local):
-    """--workload rollout_n16k_k64: the differentiable rollout.  One bench step is one
-    forward + backward pass of the K-step rollout with the soft radial distribution loss
-    (cf_rollout_forward, cf_rdf, cf_rdf_backward, cf_rollout_backward); the plain step
-    (cf_step, K steps) is timed beside it for the adjoint / forward cost ratio."""
+def run_rollout(args, rank, world, local, name="rollout_n16k_k64", steps=5, warmup=3):
+    """rollout_n16k_k64: the differentiable rollout.  One bench step is one forward + backward
+    pass of the K-step rollout with the soft radial distribution loss (cf_rollout_forward,
+    cf_rdf, cf_rdf_backward, cf_rollout_backward); the plain step (cf_step, K steps) is timed
+    beside it for the adjoint / forward cost ratio, and the adjoint kernels of a profiled
+    backward (per-step events, no graph) against the adjoint work model for their roofline.
+    Returns rank 0's record."""
     import numpy as np
     import torch
 
-    import cellflow_gb300 as cf
     from cellflow_gb300 import _lib, inputs
     from cellflow_gb300.world import ParticleSimulation
 
-    torch.cuda.set_device(local)
-    cfg = ROLLOUT[args.workload]
+    cfg = ROLLOUT[name]
     n, T, K = cfg["n"], cfg["types"], cfg["steps"]
-    w = inputs.Workload(args.workload, n=n, num_types=T, radius=cfg["radius"], steps=K, seed=cfg["seed"])
+    w = inputs.Workload(name, n=n, num_types=T, radius=cfg["radius"], steps=K, seed=cfg["seed"])
     params = w.params()
     pos, types, table = w.positions(), w.types(), w.table()
     target_table = inputs.gaussian_table(T, 0.0, 0.5, cfg["seed"] + 1)
@@ -723,11 +813,11 @@ def run_rollout(args, rank, world, local):
             ms.append(e0.elapsed_time(e1))
         return ms
 
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         sim.set_state(*s0)
         train_step()
     sim.sync()
-    reps = max(1, args.steps // 10) if args.steps >= 10 else args.steps
+    reps = max(1, steps // 10) if steps >= 10 else steps
     clocks = ClockSampler(local)
     clocks.start()
     fwd_plain = timed(lambda: sim.simulate(params, K), reps)
@@ -757,27 +847,61 @@ def run_rollout(args, rank, world, local):
             hgrad.copy_(g0, non_blocking=True)
         stream.synchronize()
         e2e.append(time.perf_counter() - t0)
+    # ---- adjoint roofline: a profiled backward (events around each adjoint step's kernels),
+    # and the work counters of the K forward states it differentiates
+    sim.set_state(*s0)
+    sim.rollout_forward(params, K, cfg["every"], None, None, None, None)
+    _lib.check(lib.cf_profile_enable(sim.handle, 1), "cf_profile_enable")
+    sim.rollout_backward(gx.data_ptr(), None, g0.data_ptr(), gv0.data_ptr())
+    prof = _lib.PhaseTimes()
+    _lib.check(lib.cf_profile_read(sim.handle, C.byref(prof)), "cf_profile_read")
+    _lib.check(lib.cf_profile_enable(sim.handle, 0), "cf_profile_enable")
+    sim.set_state(*s0)
+    c27_total, inter_total = 0, 0
+    for _ in range(K):
+        c27, _ = sim.work_counters(params)
+        sim.simulate(params, 1)
+        _, inter = sim.work_counters(params)
+        c27_total += c27
+        inter_total += inter
+    adj_flops = 9 * c27_total + 70 * inter_total + 41 * n * K
+    adj_tflops = adj_flops / (prof.adjoint_ms * 1e-3) / 1e12 if prof.adjoint_ms > 0 else None
+    peak_fp32 = C.c_double()
+    _lib.check(lib.cf_measure_fp32_peak(C.byref(peak_fp32)), "cf_measure_fp32_peak")
+    line = None
     if rank == 0:
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
-            "steps": reps, "warmup": max(args.warmup, 3), "ms_per_step": med(train),
+            "steps": reps, "warmup": max(warmup, 3), "ms_per_step": med(train),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Philox4x32-10): uniform positions, N(0,0.5) table, hidden N(0,0.5) target "
                     "table",
-            "config": {"workload": args.workload, "n": n, "types": T, "radius": cfg["radius"], "rollout_steps": K,
+            "config": {"workload": name, "n": n, "types": T, "radius": cfg["radius"], "rollout_steps": K,
                        "checkpoint_every": cfg["every"], "loss": f"MSE of the soft radial distribution "
                        f"({bins} bins, r <= {r_max})", "l2": "state smaller than L2; 256 MiB flush before each "
                        "timed pass"},
             "unit_of_step": "one forward + backward pass of the K-step rollout and its loss",
             "forward_step_ms": step_fwd, "rollout_forward_step_ms": med(fwd_roll) / K,
             "adjoint_step_ms": step_bwd, "adjoint_over_forward": step_bwd / step_fwd,
+            "roofline": {
+                "kernel": "adj_prep_kernel + adj_pair_kernel (one backward step), timed alone in a profiled "
+                          "backward",
+                "bound": "fp32", "achieved": adj_tflops, "peak": peak_fp32.value, "unit": "TFLOP/s",
+                "frac": adj_tflops / peak_fp32.value if adj_tflops else None,
+                "peak_source": "FP32 FMA chains on every SM, measured in this run (cf_measure_fp32_peak)",
+                "work_model": "9*C27 + 70*I + 41*N flops per adjoint step (include/cellflow/work_model.h)",
+                "adjoint_kernels_ms_per_step": prof.adjoint_ms / max(prof.adjoint_steps, 1),
+                "steps": int(prof.adjoint_steps),
+                "c27_per_particle_step": c27_total / (n * K),
+                "interacting_per_particle_step": inter_total / (n * K),
+            },
             "e2e": {"value": n * K / med(e2e), "unit": "particle-steps/s", "h2d_bytes_per_step": n * 16,
                     "d2h_bytes_per_step": n * 16 + 4 * (T * T + 6),
                     "path": "pinned positions in, rollout + loss + adjoint, pinned position gradients out"},
             "gpu_launches": int(launches), "clocks": clk,
-            "library": cf.__name__ + ": " + lib.cf_version().decode(),
         }
-        print(json.dumps(line), flush=True)
+    sim.close()
+    return line
 
 
 def proximity_timing(sim, w, stream, calls):
@@ -975,24 +1099,55 @@ def profile_rollout(args) -> None:
     print(json.dumps({"profile_steps": K, "workload": args.workload}))
 
 
+HEADLINE = "plain_n100k_t8"
+# the nested records of the default run: (workload, steps, warm-up steps)
+NESTED = (("blobs_n1m_t12", 20, 3), ("batched_256w", 100, 100), ("rollout_n16k_k64", 5, 3))
+
+
+def run_workload(args, rank, world, local, name, steps, warmup, cpu_seconds, extras=True):
+    from cellflow_gb300 import inputs
+
+    if name in inputs.BATCHED:
+        return run_batched(args, rank, world, local, name, steps, warmup, cpu_seconds)
+    if name in ROLLOUT:
+        return run_rollout(args, rank, world, local, name, steps, warmup)
+    return run_gb300(args, rank, world, local, name, steps, warmup, cpu_seconds, extras)
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
+    if args.workload is None:
+        args.workload = HEADLINE
+        nested = not args.no_nested
+    else:
+        nested = False
     if args.profile_steps is not None:
         profile_steps(args)
         return
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
         return
-    from cellflow_gb300 import inputs
+    import torch
 
-    if args.workload in inputs.BATCHED:
-        run_batched(args, rank, world, local)
-        return
-    if args.workload in ROLLOUT:
-        run_rollout(args, rank, world, local)
-        return
-    run_gb300(args, rank, world, local)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    line = run_workload(args, rank, world, local, args.workload, args.steps, args.warmup, args.cpu_seconds)
+    if nested:
+        # the other configurations, each with its own timing, roofline, CPU baseline and e2e
+        records = {}
+        for name, steps, warmup in NESTED:
+            records[name] = run_workload(args, rank, world, local, name, steps, warmup, args.cpu_seconds / 2,
+                                         extras=False)
+        if line is not None:
+            line["workloads"] = records
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 if __name__ == "__main__":

@@ -105,6 +105,8 @@ class PhaseTimes(C.Structure):
         ("force_ms", C.c_double),
         ("steps", C.c_longlong),
         ("launches", C.c_longlong),
+        ("adjoint_ms", C.c_double),
+        ("adjoint_steps", C.c_longlong),
     ]
 
 

@@ -24,6 +24,7 @@ namespace {
 thread_local std::string g_error;
 
 constexpr int kMaxCells = 1 << 22;        // cap of the step and proximity grids
+constexpr int kProfRing = 1024;           // event triples of profiled steps in flight
 constexpr int kMaxCanonicalCells = 1 << 24;  // cap of the work-model grid
 
 uint64_t splitmix64(uint64_t& s)
@@ -471,23 +472,38 @@ void apply_worlds(Grid& g, int worlds)
 // One step's launches on the world's stream: cell list, then the fused force,
 // density and integrator kernel; with the three profiling events when prof
 // (recorded as external event nodes when the stream is being captured).
-int enqueue_step(cf_world* w, const StepConsts& c, int prof)
+// The step's two phases.  The cell list leaves the sorted keys and values in
+// buffer `which` of the scratch pair, a function of the grid alone
+// (cell_list_csr_buffer), which the force kernel reads.
+int enqueue_cell_list(cf_world* w, const StepConsts& c, int* which)
 {
-    if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[0], w->stream, cudaEventRecordExternal));
-    int which = 0;
     Scratch& s = w->s;
     CF_CUDA(launch_cell_list_csr(w->pos, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, s.items, s.n_items, w->err,
-                                 &which, w->stream));
-    if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[1], w->stream, cudaEventRecordExternal));
-    CF_CUDA(launch_step_force(c, w->tables, s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.items,
-                              s.n_items, max_step_items(w->n, c.grid), w->pos, w->vel, w->acc, w->counts,
-                              w->stream));
-    if (prof) CF_CUDA(cudaEventRecordWithFlags(w->prof_ev[2], w->stream, cudaEventRecordExternal));
+                                 which, w->stream));
     return CF_OK;
 }
 
-// The one-step graph for these constants, captured on first use and again
-// whenever the constants or the scratch buffers change.
+int enqueue_force(cf_world* w, const StepConsts& c, int which)
+{
+    Scratch& s = w->s;
+    CF_CUDA(launch_step_force(c, w->tables, s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.items,
+                              s.n_items, max_step_items(w->n, c.grid), w->pos, w->vel, w->acc, w->counts,
+                              w->stream));
+    return CF_OK;
+}
+
+int enqueue_step(cf_world* w, const StepConsts& c, int prof)
+{
+    (void)prof;
+    int which = 0;
+    int rc = enqueue_cell_list(w, c, &which);
+    if (rc) return rc;
+    return enqueue_force(w, c, which);
+}
+
+// The one-step graph for these constants (prof = 1: the cell list alone),
+// captured on first use and again whenever the constants or the scratch
+// buffers change.
 int step_graph(cf_world* w, const StepConsts& c, int prof, cudaGraphExec_t* out)
 {
     const void* bufs = w->s.cell_start;
@@ -501,7 +517,8 @@ int step_graph(cf_world* w, const StepConsts& c, int prof, cudaGraphExec_t* out)
     }
     cudaGraph_t graph = nullptr;
     CF_CUDA(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_step(w, c, prof);
+    int which = 0;
+    int rc = prof ? enqueue_cell_list(w, c, &which) : enqueue_step(w, c, 0);
     cudaError_t e = cudaStreamEndCapture(w->stream, &graph);
     if (rc) {
         if (graph) cudaGraphDestroy(graph);
@@ -515,6 +532,31 @@ int step_graph(cf_world* w, const StepConsts& c, int prof, cudaGraphExec_t* out)
     w->graph_key[prof] = c;
     w->graph_bufs[prof] = bufs;
     *out = w->graph[prof];
+    return CF_OK;
+}
+
+// Adds the phase times of the `count` oldest profiled steps of the ring (waiting
+// for each one's last event) to the world's totals.
+int harvest_profile(cf_world* w, int count)
+{
+    const int size = (int)w->prof_ring.size();
+    for (int k = 0; k < count && w->prof_pending > 0; k++) {
+        const int slot = ((w->prof_head - w->prof_pending) % size + size) % size;
+        const auto& ev = w->prof_ring[slot];
+        CF_CUDA(cudaEventSynchronize(ev[2]));
+        float a = 0.0f, b = 0.0f;
+        CF_CUDA(cudaEventElapsedTime(&a, ev[0], ev[1]));
+        if (w->prof_kind[slot] == 0) {
+            CF_CUDA(cudaEventElapsedTime(&b, ev[1], ev[2]));
+            w->prof_cell_ms += a;
+            w->prof_force_ms += b;
+            w->prof_steps++;
+        } else {
+            w->prof_adj_ms += a;
+            w->prof_adj_steps++;
+        }
+        w->prof_pending--;
+    }
     return CF_OK;
 }
 
@@ -794,8 +836,10 @@ int cf_destroy(cf_world* w)
 {
     if (!w) return CF_OK;
     if (w->stream) cudaStreamSynchronize(w->stream);
-    for (int k = 0; k < 3; k++)
-        if (w->prof_ev[k]) cudaEventDestroy(w->prof_ev[k]);
+    for (auto& ev : w->prof_ring)
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    w->prof_ring.clear();
     drop_graphs(w);
     free_particles(w);
     dev_free(w->err);
@@ -1127,24 +1171,40 @@ int cf_step(cf_world* w, const cf_step_params* p, int nsteps)
     }
     const long long launches = cell_list_csr_launches(w->n, c.grid, true) + step_launches(w->n);
     for (int s = 0; s < nsteps; s++) {
-        if (exec) {
-            CF_CUDA(cudaGraphLaunch(exec, w->stream));
-            note_launches(w->stream, w->graph_kernels[prof]);
-        } else {
-            rc = enqueue_step(w, c, prof);
+        if (!prof) {
+            if (exec) {
+                CF_CUDA(cudaGraphLaunch(exec, w->stream));
+                note_launches(w->stream, w->graph_kernels[0]);
+            } else {
+                rc = enqueue_step(w, c, 0);
+                if (rc) return rc;
+            }
+            continue;
+        }
+        // profiled: events from the ring around the cell list (its graph) and the force kernel
+        if (w->prof_pending == (int)w->prof_ring.size()) {
+            rc = harvest_profile(w, 1);
             if (rc) return rc;
         }
-        if (prof) {
-            // serialised steps: read this step's phase times
-            CF_CUDA(cudaEventSynchronize(w->prof_ev[2]));
-            float a = 0.0f, b = 0.0f;
-            CF_CUDA(cudaEventElapsedTime(&a, w->prof_ev[0], w->prof_ev[1]));
-            CF_CUDA(cudaEventElapsedTime(&b, w->prof_ev[1], w->prof_ev[2]));
-            w->prof_cell_ms += a;
-            w->prof_force_ms += b;
-            w->prof_steps++;
-            w->prof_launches += launches;
+        const auto& ev = w->prof_ring[w->prof_head];
+        w->prof_kind[w->prof_head] = 0;
+        w->prof_head = (w->prof_head + 1) % (int)w->prof_ring.size();
+        w->prof_pending++;
+        CF_CUDA(cudaEventRecord(ev[0], w->stream));
+        int which = 0;
+        if (exec) {
+            CF_CUDA(cudaGraphLaunch(exec, w->stream));
+            note_launches(w->stream, w->graph_kernels[1]);
+            which = cell_list_csr_buffer(w->n, c.grid);
+        } else {
+            rc = enqueue_cell_list(w, c, &which);
+            if (rc) return rc;
         }
+        CF_CUDA(cudaEventRecord(ev[1], w->stream));
+        rc = enqueue_force(w, c, which);
+        if (rc) return rc;
+        CF_CUDA(cudaEventRecord(ev[2], w->stream));
+        w->prof_launches += launches;
     }
     return CF_OK;
 }
@@ -1354,11 +1414,18 @@ int cf_profile_enable(cf_world* w, int on)
     int rc = check_world(w);
     if (rc) return rc;
     CF_CUDA(cudaStreamSynchronize(w->stream));
-    for (int k = 0; k < 3; k++)
-        if (!w->prof_ev[k]) CF_CUDA(cudaEventCreate(&w->prof_ev[k]));
+    if (w->prof_ring.empty()) {
+        w->prof_ring.resize(kProfRing);
+        w->prof_kind.assign(kProfRing, 0);
+        for (auto& ev : w->prof_ring)
+            for (auto& e : ev) e = nullptr;
+        for (auto& ev : w->prof_ring)
+            for (auto& e : ev) CF_CUDA(cudaEventCreate(&e));
+    }
     w->profiling = on != 0;
-    w->prof_cell_ms = w->prof_force_ms = 0.0;
-    w->prof_steps = w->prof_launches = 0;
+    w->prof_head = w->prof_pending = 0;
+    w->prof_cell_ms = w->prof_force_ms = w->prof_adj_ms = 0.0;
+    w->prof_steps = w->prof_launches = w->prof_adj_steps = 0;
     return CF_OK;
 }
 
@@ -1368,12 +1435,16 @@ int cf_profile_read(cf_world* w, cf_phase_times* out)
     if (rc) return rc;
     if (!out) return fail(CF_ERR_INVALID, "null output");
     CF_CUDA(cudaStreamSynchronize(w->stream));
+    rc = harvest_profile(w, w->prof_pending);
+    if (rc) return rc;
     out->cell_list_ms = w->prof_cell_ms;
     out->force_ms = w->prof_force_ms;
     out->steps = w->prof_steps;
     out->launches = w->prof_launches;
-    w->prof_cell_ms = w->prof_force_ms = 0.0;
-    w->prof_steps = w->prof_launches = 0;
+    out->adjoint_ms = w->prof_adj_ms;
+    out->adjoint_steps = w->prof_adj_steps;
+    w->prof_cell_ms = w->prof_force_ms = w->prof_adj_ms = 0.0;
+    w->prof_steps = w->prof_launches = w->prof_adj_steps = 0;
     return CF_OK;
 }
 
@@ -2091,19 +2162,39 @@ int adjoint_segment(cf_world* w, const StepConsts& c, int seg, const SegBuf& b, 
     const int len = std::min(r.every, r.steps - seg * r.every);
     Scratch& s = w->s;
     for (int t = len - 1; t >= 0; t--) {
+        const float4* ps = s.pos_sorted;
+        const uint32_t *ks = nullptr, *vs = nullptr, *off = s.cell_off;
         if (lists) {
-            CF_CUDA(launch_adjoint_step(c, w->tables, b.sorted + n * t, b.keys + n * t, b.vals + n * t,
-                                        b.off + r.lists_cells * t, b.vel + n * t, b.cnt + n * t,
-                                        b.cnt + n * (t + 1), r.gx, r.gv, r.gf_sorted, r.ga_sorted, r.gacc,
-                                        w->stream));
-            continue;
+            ps = b.sorted + n * t;
+            ks = b.keys + n * t;
+            vs = b.vals + n * t;
+            off = b.off + r.lists_cells * t;
+        } else {
+            int which = 0;
+            CF_CUDA(launch_cell_list_csr(b.pos + n * t, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, nullptr,
+                                         nullptr, w->err, &which, w->stream));
+            ks = s.keys[which];
+            vs = s.vals[which];
         }
-        int which = 0;
-        CF_CUDA(launch_cell_list_csr(b.pos + n * t, w->n, c.grid, c.ext, w->num_types, s, s.cell_off, nullptr,
-                                     nullptr, w->err, &which, w->stream));
-        CF_CUDA(launch_adjoint_step(c, w->tables, s.pos_sorted, s.keys[which], s.vals[which], s.cell_off,
-                                    b.vel + n * t, b.cnt + n * t, b.cnt + n * (t + 1), r.gx, r.gv, r.gf_sorted,
-                                    r.ga_sorted, r.gacc, w->stream));
+        const std::array<cudaEvent_t, 3>* ev = nullptr;
+        if (w->profiling) {
+            // profiled backward (no graph, no overlap): events around the adjoint kernels
+            if (w->prof_pending == (int)w->prof_ring.size()) {
+                const int e = harvest_profile(w, 1);
+                if (e) return e;
+            }
+            ev = &w->prof_ring[w->prof_head];
+            w->prof_kind[w->prof_head] = 1;
+            w->prof_head = (w->prof_head + 1) % (int)w->prof_ring.size();
+            w->prof_pending++;
+            CF_CUDA(cudaEventRecord((*ev)[0], w->stream));
+        }
+        CF_CUDA(launch_adjoint_step(c, w->tables, ps, ks, vs, off, b.vel + n * t, b.cnt + n * t, b.cnt + n * (t + 1),
+                                    r.gx, r.gv, r.gf_sorted, r.ga_sorted, r.gacc, w->stream));
+        if (ev) {
+            CF_CUDA(cudaEventRecord((*ev)[1], w->stream));
+            CF_CUDA(cudaEventRecord((*ev)[2], w->stream));
+        }
     }
     return CF_OK;
 }
@@ -2273,7 +2364,7 @@ int cf_rollout_backward(cf_world* w, const float* d_gpos4, const float* d_gvel4,
         CF_CUDA(cudaMemcpyAsync(r.gv, d_gvel4, sizeof(float4) * n, cudaMemcpyDeviceToDevice, w->stream));
     else
         CF_CUDA(cudaMemsetAsync(r.gv, 0, sizeof(float4) * n, w->stream));
-    if (w->use_graphs && w->stream != nullptr) {
+    if (w->use_graphs && w->stream != nullptr && !w->profiling) {
         const void* bufs = w->s.cell_start;
         const bool same = r.bwd_graph && r.bwd_steps == r.steps && r.bwd_every == r.every && r.bwd_bufs == bufs &&
                           r.bwd_lists == r.seg_off && std::memcmp(&r.bwd_key, &c, sizeof(c)) == 0;

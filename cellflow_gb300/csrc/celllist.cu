@@ -687,6 +687,16 @@ cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const 
     return cudaGetLastError();
 }
 
+// The buffer of the scratch pair (keys, vals)[k] that launch_cell_list_csr
+// leaves the sorted order in: a function of the grid and the count alone.
+int cell_list_csr_buffer(int n, const Grid& g)
+{
+    if (cell_list_tiles(g) != 0) return 1;
+    if (n <= 0) return 0;
+    const int passes = std::max(1, (g.key_bits + 7) / 8);
+    return passes & 1;
+}
+
 int cell_list_csr_launches(int n, const Grid& g, bool with_plan)
 {
     if (cell_list_tiles(g) == 0) {

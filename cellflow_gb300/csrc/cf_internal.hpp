@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -242,13 +243,20 @@ struct cf_world {
     int uploaded_types = -1;
     float uploaded_extent = -1.0f;
     cf::PairTables host_tables;
-    // phase profiling (cf_profile_enable): events start / after cell list / after force
+    // phase profiling (cf_profile_enable): per profiled step a triple of events
+    // (start, after the cell list, after the force kernel) from a ring; the
+    // times are read when a slot is reused or at cf_profile_read, so profiled
+    // steps are not serialised.  Adjoint steps of a profiled backward use the
+    // same ring (kind 1: start and end of their kernels).
     bool profiling = false;
-    cudaEvent_t prof_ev[3] = {nullptr, nullptr, nullptr};
-    double prof_cell_ms = 0.0, prof_force_ms = 0.0;
-    long long prof_steps = 0, prof_launches = 0;
-    // one-step CUDA graphs (index 1: with the profiling events), re-captured
-    // when the step constants or buffers change
+    std::vector<std::array<cudaEvent_t, 3>> prof_ring;
+    std::vector<unsigned char> prof_kind;  // per ring slot: 0 a step, 1 an adjoint step
+    int prof_head = 0, prof_pending = 0;
+    double prof_cell_ms = 0.0, prof_force_ms = 0.0, prof_adj_ms = 0.0;
+    long long prof_steps = 0, prof_launches = 0, prof_adj_steps = 0;
+    // one-step CUDA graphs (index 1: the cell list alone, for profiled steps,
+    // whose force kernel is launched between the events), re-captured when the
+    // step constants or buffers change
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long graph_kernels[2] = {0, 0};  // kernel nodes of graph[k]
     cf::StepConsts graph_key[2];
@@ -319,6 +327,7 @@ int cell_list_launches(int n, int key_bits);
 cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
                                  Scratch& s, uint32_t* cell_off, Item* items, int* n_items, int* err, int* which,
                                  cudaStream_t st);
+int cell_list_csr_buffer(int n, const Grid& g);
 int cell_list_csr_launches(int n, const Grid& g, bool with_plan);
 int cell_list_tiles(const Grid& g);  // 0 when the rows are longer than a tile
 // csr: cell_start = CSR offsets and cell_end = offsets + 1 (rows read as

@@ -448,16 +448,21 @@ int cf_preset_write(cf_world* w, const cf_preset* p, char* buf, size_t cap, size
 
 /* Device time of the step's phases, accumulated over the steps run since
  * profiling was enabled or last read, from CUDA events recorded on the
- * world's stream around each phase. */
+ * world's stream around each phase; and of the adjoint steps of
+ * cf_rollout_backward (their per-particle and pair kernels), which run one
+ * after another, outside any graph, while profiling is on. */
 typedef struct cf_phase_times {
-    double cell_list_ms; /* hash + radix sort + start/end + sorted snapshot */
-    double force_ms;     /* force + density + integrator kernel           */
-    long long steps;     /* steps covered                                  */
-    long long launches;  /* kernel launches of the library in those steps  */
+    double cell_list_ms;     /* hash + radix sort + start/end + sorted snapshot */
+    double force_ms;         /* force + density + integrator kernel           */
+    long long steps;         /* steps covered                                  */
+    long long launches;      /* kernel launches of the library in those steps  */
+    double adjoint_ms;       /* adj_prep + adj_pair kernels of backward steps  */
+    long long adjoint_steps; /* backward steps covered                         */
 } cf_phase_times;
 
 /* No counterpart in the reference (it had only a frame counter,
- * CellFlowWidget.cpp:705-713).  Enabling adds two events per phase. */
+ * CellFlowWidget.cpp:705-713).  Enabling adds events around each phase (no
+ * synchronisation: the times are read when cf_profile_read is called). */
 int cf_profile_enable(cf_world* w, int on);
 int cf_profile_read(cf_world* w, cf_phase_times* out);
 /* Measured FP32 FMA throughput of the current device in TFLOP/s (an FMA

@@ -1,5 +1,6 @@
 /*
- * work_model.h - frozen algorithmic work of one CellFlow step.
+ * work_model.h - frozen algorithmic work of one CellFlow step (and of one
+ * adjoint step of the differentiable rollout).
  *
  * These constants define the "algorithmic" flops and bytes that roofline
  * figures divide by a measured time.  They count the work of the reference
@@ -21,6 +22,19 @@
  *   read + write), reorder gather 68 (index 4 + pos 16 + vel 16 read,
  *   pos 16 + vel 16 written), cell start/end 4.
  *
+ * Adjoint step of the differentiable rollout (FP32 flops per backward step):
+ *     W_adj = 9 * C27 + 70 * I + 41 * N
+ *   9  per candidate: the forward's displacement, |d|^2 and +1e-4.
+ *   70 per interacting pair: 1/dist, dist, r (3), the exponent and exp (3),
+ *        the force n = R e - A r (3) and its derivative n' (4), n/dist (1),
+ *        the Hessian coefficient (n' dist - n)/dist^3 (5), the adjoint weight
+ *        F_ji g_j - F_ij g_i (9), its projection on d (5), the position
+ *        gradient phi w + h (d.w) d accumulated (13), g_i.d/dist (6), the
+ *        force-table gradient (2), the repulsion, attraction and k gradients
+ *        (3 + 2 + 4), the force itself for the scale gradients (7).
+ *   41 per particle: the per-particle adjoint of the density scale and the
+ *        integrator (26) and the warp's finish of the home (15).
+ *
  * Integrator, when not fused (bytes per particle): 88.
  * Proximity graph (bytes per particle): 16 + 8 per emitted edge.
  */
@@ -30,6 +44,10 @@
 #define CF_WM_FLOPS_PER_CANDIDATE 9
 #define CF_WM_FLOPS_PER_INTERACTION 17
 #define CF_WM_FLOPS_PER_PARTICLE 25
+
+#define CF_WM_ADJ_FLOPS_PER_CANDIDATE 9
+#define CF_WM_ADJ_FLOPS_PER_INTERACTION 70
+#define CF_WM_ADJ_FLOPS_PER_PARTICLE 41
 
 #define CF_WM_CELL_BYTES_PER_PARTICLE 112
 #define CF_WM_CELL_BYTES_PER_CELL 8
@@ -42,6 +60,13 @@ static inline double cf_wm_force_flops(double c27, double interacting, double n)
 {
     return CF_WM_FLOPS_PER_CANDIDATE * c27 + CF_WM_FLOPS_PER_INTERACTION * interacting +
            CF_WM_FLOPS_PER_PARTICLE * n;
+}
+
+/* Adjoint flops of one backward step. */
+static inline double cf_wm_adjoint_flops(double c27, double interacting, double n)
+{
+    return CF_WM_ADJ_FLOPS_PER_CANDIDATE * c27 + CF_WM_ADJ_FLOPS_PER_INTERACTION * interacting +
+           CF_WM_ADJ_FLOPS_PER_PARTICLE * n;
 }
 
 /* Cell-list bytes of one step. */

@@ -36,6 +36,9 @@ def test_host_cpu_model_is_recorded():
 def test_default_command_line(monkeypatch):
     monkeypatch.setattr(sys, "argv", ["bench.py"])
     a = bench.parse_args()
-    assert a.gpus == 1 and a.impl == "gb300" and a.workload == "plain_n100k_t8"
-    assert a.warmup >= 3 and a.steps >= 1
+    # no workload named: the 100k headline with the other configurations nested in its record
+    assert a.gpus == 1 and a.impl == "gb300" and a.workload is None and not a.no_nested
+    assert bench.HEADLINE == "plain_n100k_t8"
+    assert [name for name, _, _ in bench.NESTED] == ["blobs_n1m_t12", "batched_256w", "rollout_n16k_k64"]
+    assert a.warmup >= 3 and a.steps >= 1 and all(w >= 3 for _, _, w in bench.NESTED)
     assert a.profile_steps is None and a.variant is None
