@@ -147,6 +147,10 @@ _SIGNATURES = {
     "cf_last_error": (C.c_char_p, []),
     "cf_version": (C.c_char_p, []),
     "cf_kernel_launches": (C.c_longlong, []),
+    "cf_set_device_memory_limit": (C.c_int, [C.c_size_t]),
+    "cf_device_memory_in_use": (C.c_int, [_P(C.c_size_t)]),
+    "cf_inject_cuda_error": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
+    "cf_injection_pending": (C.c_int, []),
     "cf_default_params": (None, [_P(StepParams)]),
     "cf_create": (C.c_int, [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_uint64, _P(_W)]),
     "cf_destroy": (C.c_int, [_W]),

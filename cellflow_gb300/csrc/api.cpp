@@ -12,7 +12,9 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "cf_internal.hpp"
@@ -48,21 +50,77 @@ bool finite_positive(float v) { return std::isfinite(v) && v > 0.0f; }
 int check_world(const cf_world* w)
 {
     if (!w) return fail(CF_ERR_INVALID, "null world");
+    if (w->broken)
+        return fail(CF_ERR_INVALID,
+                    "the world lost its particle buffers when a reallocation failed; call cf_set_particle_count "
+                    "again or destroy it");
     return CF_OK;
+}
+
+// Device memory held by the library (every buffer goes through dev_alloc),
+// under an optional cap (cf_set_device_memory_limit, 0 = none): a request that
+// would exceed it fails like cudaMalloc out of memory.
+std::mutex g_mem_mu;
+std::unordered_map<void*, size_t> g_mem_sizes;
+size_t g_mem_live = 0;
+size_t g_mem_limit = 0;
+thread_local bool g_mem_capped = false;  // the last allocation failure came from the cap
+
+cudaError_t raw_alloc(void** p, size_t bytes)
+{
+    *p = nullptr;
+    g_mem_capped = false;
+    {
+        std::lock_guard<std::mutex> lock(g_mem_mu);
+        if (g_mem_limit != 0 && g_mem_live + bytes > g_mem_limit) {
+            g_mem_capped = true;
+            return cudaErrorMemoryAllocation;
+        }
+    }
+    const cudaError_t inj = injected_error("cudaMalloc");
+    if (inj != cudaSuccess) return inj;
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return e;
+    }
+    std::lock_guard<std::mutex> lock(g_mem_mu);
+    g_mem_sizes[*p] = bytes;
+    g_mem_live += bytes;
+    return cudaSuccess;
 }
 
 template <typename T>
 cudaError_t dev_alloc(T** p, size_t count)
 {
-    *p = nullptr;
     if (count == 0) count = 1;
-    return cudaMalloc((void**)p, sizeof(T) * count);
+    void* q = nullptr;
+    const cudaError_t e = raw_alloc(&q, sizeof(T) * count);
+    *p = static_cast<T*>(q);
+    return e;
 }
 
 void dev_free(void* p)
 {
-    if (p) cudaFree(p);
+    if (!p) return;
+    {
+        std::lock_guard<std::mutex> lock(g_mem_mu);
+        auto it = g_mem_sizes.find(p);
+        if (it != g_mem_sizes.end()) {
+            g_mem_live -= it->second;
+            g_mem_sizes.erase(it);
+        }
+    }
+    cudaFree(p);
 }
+
+// The armed injection: the next `skip` matching sites pass, the one after
+// returns `error` (once).
+std::mutex g_inj_mu;
+std::string g_inj_site;
+int g_inj_skip = 0;
+cudaError_t g_inj_error = cudaSuccess;
+std::atomic<bool> g_inj_armed{false};
 
 void apply_worlds(Grid& g, int worlds);
 
@@ -255,22 +313,36 @@ int ensure_aos(cf_world* w)
     return CF_OK;
 }
 
+// Two buffers allocated together or not at all (a lazily allocated pair is
+// tested by its first member).
+template <typename A, typename B>
+int alloc_pair(A** a, size_t na, B** b, size_t nb)
+{
+    A* x = nullptr;
+    B* y = nullptr;
+    cudaError_t e = dev_alloc(&x, na);
+    if (e == cudaSuccess) e = dev_alloc(&y, nb);
+    if (e != cudaSuccess) {
+        dev_free(x);
+        return cuda_fail(e, "dev_alloc(scratch pair)");
+    }
+    *a = x;
+    *b = y;
+    return CF_OK;
+}
+
 int ensure_prox(cf_world* w)
 {
     Scratch& s = w->s;
     if (s.prox_slots) return CF_OK;
-    CF_CUDA(dev_alloc(&s.prox_slots, (size_t)w->n * CF_MAX_PROX_CONN));
-    CF_CUDA(dev_alloc(&s.prox_count, (size_t)w->n + 1));
-    return CF_OK;
+    return alloc_pair(&s.prox_slots, (size_t)w->n * CF_MAX_PROX_CONN, &s.prox_count, (size_t)w->n + 1);
 }
 
 int ensure_mesh(cf_world* w)
 {
     Scratch& s = w->s;
     if (s.mesh_slots) return CF_OK;
-    CF_CUDA(dev_alloc(&s.mesh_slots, (size_t)w->n * CF_MESH_MAX_CONN));
-    CF_CUDA(dev_alloc(&s.mesh_count, (size_t)w->n + 1));
-    return CF_OK;
+    return alloc_pair(&s.mesh_slots, (size_t)w->n * CF_MESH_MAX_CONN, &s.mesh_count, (size_t)w->n + 1);
 }
 
 // Staging for index output copied to host memory: grows to the largest
@@ -601,7 +673,26 @@ int fail(int code, const std::string& msg)
 int cuda_fail(cudaError_t e, const char* what)
 {
     g_error = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation && g_mem_capped) {
+        g_error += " (the library's device memory limit of " + std::to_string(g_mem_limit) +
+                   " bytes would be exceeded; cf_set_device_memory_limit)";
+        g_mem_capped = false;
+    }
     return e == cudaErrorMemoryAllocation ? CF_ERR_ALLOC : CF_ERR_CUDA;
+}
+
+cudaError_t injected_error(const char* site)
+{
+    if (!g_inj_armed.load(std::memory_order_relaxed)) return cudaSuccess;
+    std::lock_guard<std::mutex> lock(g_inj_mu);
+    if (!g_inj_armed.load(std::memory_order_relaxed) || std::strstr(site, g_inj_site.c_str()) == nullptr)
+        return cudaSuccess;
+    if (g_inj_skip > 0) {
+        g_inj_skip--;
+        return cudaSuccess;
+    }
+    g_inj_armed.store(false, std::memory_order_relaxed);
+    return g_inj_error;
 }
 
 namespace {
@@ -762,6 +853,38 @@ const char* cf_version(void) { return "cellflow-gb300 0.1 (sm_103a)"; }
 
 long long cf_kernel_launches(void) { return launch_tally(); }
 
+int cf_set_device_memory_limit(size_t bytes)
+{
+    std::lock_guard<std::mutex> lock(g_mem_mu);
+    g_mem_limit = bytes;
+    return CF_OK;
+}
+
+int cf_device_memory_in_use(size_t* bytes)
+{
+    if (!bytes) return fail(CF_ERR_INVALID, "null output");
+    std::lock_guard<std::mutex> lock(g_mem_mu);
+    *bytes = g_mem_live;
+    return CF_OK;
+}
+
+int cf_inject_cuda_error(const char* site, int cuda_error, int skip)
+{
+    std::lock_guard<std::mutex> lock(g_inj_mu);
+    if (!site) {
+        g_inj_armed.store(false);
+        return CF_OK;
+    }
+    if (cuda_error <= 0 || skip < 0) return fail(CF_ERR_INVALID, "cuda_error must be a cudaError_t > 0, skip >= 0");
+    g_inj_site = site;
+    g_inj_error = static_cast<cudaError_t>(cuda_error);
+    g_inj_skip = skip;
+    g_inj_armed.store(true);
+    return CF_OK;
+}
+
+int cf_injection_pending(void) { return g_inj_armed.load() ? 1 : 0; }
+
 void cf_default_params(cf_step_params* p)
 {
     if (!p) return;
@@ -887,15 +1010,21 @@ int cf_num_particle_types(const cf_world* w, int* t)
 
 int cf_set_particle_count(cf_world* w, int n, uint64_t seed)
 {
-    int rc = check_world(w);
-    if (rc) return rc;
+    if (!w) return fail(CF_ERR_INVALID, "null world");  // a broken world may be reallocated
     if (n < 0) return fail(CF_ERR_INVALID, "particle count must be >= 0");
-    if (n == w->n) return CF_OK;  // ParticleSimulation.cu:565
+    if (n == w->n && !w->broken) return CF_OK;  // ParticleSimulation.cu:565
     CF_CUDA(cudaStreamSynchronize(w->stream));
     free_particles(w);
     w->n = n;
-    rc = alloc_particles(w);
-    if (rc) return rc;
+    int rc = alloc_particles(w);
+    if (rc) {
+        // no half-allocated world: every later call reports this until a reallocation succeeds
+        const std::string msg = cf_last_error();
+        free_particles(w);
+        w->broken = true;
+        return fail(rc, msg);
+    }
+    w->broken = false;
     rc = respawn(w, seed, 2000.0f);
     if (rc) return rc;
     return sync_and_check(w);
@@ -2072,9 +2201,11 @@ int ensure_rdf(cf_world* w)
 {
     Rollout& r = w->ro;
     if (r.rdf_pos) return CF_OK;
-    CF_CUDA(dev_alloc(&r.rdf_pos, (size_t)std::max(w->n, 1)));
-    CF_CUDA(dev_alloc(&r.rdf_acc, (size_t)kRdfMaxEntries));
-    CF_CUDA(dev_alloc(&r.type_count, (size_t)CF_MAX_TYPES));
+    if (!r.rdf_acc) {
+        const int rc = alloc_pair(&r.rdf_acc, (size_t)kRdfMaxEntries, &r.type_count, (size_t)CF_MAX_TYPES);
+        if (rc) return rc;
+    }
+    CF_CUDA(dev_alloc(&r.rdf_pos, (size_t)std::max(w->n, 1)));  // last: it marks the set complete
     return CF_OK;
 }
 

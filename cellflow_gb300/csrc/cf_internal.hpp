@@ -262,6 +262,7 @@ struct cf_world {
     cf::StepConsts graph_key[2];
     const void* graph_bufs[2] = {nullptr, nullptr};
     bool use_graphs = true;
+    bool broken = false;  // a particle reallocation failed: no buffers until one succeeds
     int force_variant = 0;  // force-kernel variant, chosen by cf_autotune_step
     // a captured multi-step graph (cf_batch_capture) and the constants it was captured with
     cudaGraphExec_t batch_graph = nullptr;
@@ -292,9 +293,14 @@ void note_launches(cudaStream_t st, long long k = 1);
 long long launch_tally();
 // Kernel nodes of a captured graph.
 cudaError_t graph_kernel_count(cudaGraph_t graph, long long* kernels);
+// Host-side fault injection (cf_inject_cuda_error): the error armed for a
+// call site whose text contains the armed substring, else cudaSuccess.  The
+// call itself is then not made.
+cudaError_t injected_error(const char* site);
 #define CF_CUDA(call)                                                   \
     do {                                                                \
-        cudaError_t cf_e_ = (call);                                     \
+        cudaError_t cf_e_ = ::cf::injected_error(#call);                \
+        if (cf_e_ == cudaSuccess) cf_e_ = (call);                       \
         if (cf_e_ != cudaSuccess) return ::cf::cuda_fail(cf_e_, #call); \
     } while (0)
 

@@ -108,6 +108,26 @@ const char* cf_version(void);
  * CUDA graph it launches (a step, a batch replay, a selection pass, a rollout
  * backward).  The difference around a region is that region's launch count. */
 long long cf_kernel_launches(void);
+
+/* ---- host-side fault injection and limits (no counterpart in the reference,
+ * whose CUDA_CHECK printed and exited, ParticleSimulation.cu:10-18) -------- */
+
+/* Cap on the device memory the library itself holds (every buffer of every
+ * world and batch), in bytes; 0 removes the cap.  An allocation that would
+ * exceed it fails as cudaMalloc out of memory would: CF_ERR_ALLOC, with the
+ * cap named in cf_last_error().  Lowering it frees nothing already held. */
+int cf_set_device_memory_limit(size_t bytes);
+/* Device memory the library holds now, in bytes. */
+int cf_device_memory_in_use(size_t* bytes);
+/* Arms a one-shot injected CUDA error: the CUDA call sites whose text
+ * contains `site` (e.g. "cudaMalloc", "cudaStreamSynchronize",
+ * "launch_step_force") pass `skip` times, then the next one returns
+ * `cuda_error` (a cudaError_t value) without making the call, and the
+ * library reports it as it would a real failure (CF_ERR_CUDA, or CF_ERR_ALLOC
+ * for cudaErrorMemoryAllocation).  NULL disarms.  Process-wide. */
+int cf_inject_cuda_error(const char* site, int cuda_error, int skip);
+/* 1 while an injected error is armed and has not fired, else 0. */
+int cf_injection_pending(void);
 /* SimulationParams defaults (SimulationParams.h:15-29). */
 void cf_default_params(cf_step_params* p);
 
@@ -127,7 +147,10 @@ int cf_sync(cf_world* w);
 int cf_particle_count(const cf_world* w, int* n);
 int cf_num_particle_types(const cf_world* w, int* t);
 
-/* setParticleCount (ParticleSimulation.cu:564-572): reallocates and respawns. */
+/* setParticleCount (ParticleSimulation.cu:564-572): reallocates and respawns.
+ * If the reallocation fails (CF_ERR_ALLOC), the world holds no particle buffers
+ * and every other call on it returns CF_ERR_INVALID until a later
+ * cf_set_particle_count succeeds (or cf_destroy). */
 int cf_set_particle_count(cf_world* w, int n, uint64_t seed);
 /* setNumParticleTypes (ParticleSimulation.cu:574-579): new type count, new
  * seeded raw table and radius table, respawn. */

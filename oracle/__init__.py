@@ -67,18 +67,25 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
+def reference_root() -> Path:
+    """The reference checkout: $CELLFLOW_REFERENCE, else a directory named `reference` beside
+    this repository."""
+    env = os.environ.get("CELLFLOW_REFERENCE")
+    return Path(env) if env else HERE.parent.parent / "reference"
+
+
 def build_ref(gpu: bool = True) -> bool:
     """Run build_ref.sh; True when oracle/_ref/libcfref.so exists afterwards."""
     inputs = [REF_DIR / "ref_step_kernel.inc", HERE / "ref_host_shim.cu", HERE / "ref_gpu_shim.cu",
               HERE / "build_ref.sh", REF_DIR / "ref_mesh_kernel.inc"]
     outputs = [REF_LIB] + ([REF_GPU_LIB] if gpu else [])
-    ref_src = Path(os.environ.get("CELLFLOW_REFERENCE", "/root/reference")) / "cuda-native/src/ParticleSimulation.cu"
+    ref_src = reference_root() / "cuda-native/src/ParticleSimulation.cu"
     if not ref_src.exists() and all(p.exists() for p in outputs + inputs[:1]):
         newest = max(p.stat().st_mtime for p in inputs if p.exists())
         if all(o.stat().st_mtime >= newest for o in outputs):
             return True
     args = [str(HERE / "build_ref.sh")] + ([] if gpu else ["--no-gpu"])
-    subprocess.run(["sh", *args], check=True)
+    subprocess.run(["sh", *args], check=True, env=dict(os.environ, CELLFLOW_REFERENCE=str(reference_root())))
     return REF_LIB.exists()
 
 

@@ -14,7 +14,8 @@
 set -eu
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
-REF=${CELLFLOW_REFERENCE:-/root/reference}
+# the reference checkout: $CELLFLOW_REFERENCE, else `reference` beside this repository
+REF=${CELLFLOW_REFERENCE:-$HERE/../../reference}
 SRC="$REF/cuda-native/src/ParticleSimulation.cu"
 HDR="$REF/cuda-native/include/SimulationParams.h"
 SRC_SHA=ce1da0c9b70d91365ead243f87d12a363f21474272e6b89410b45030274f7fcd

@@ -58,9 +58,10 @@ def ref_rollout(pos, types, table, radio, params, steps):
     return snaps
 
 
-def main(ref_root: str = "/root/reference") -> None:
+def main(ref_root: str | None = None) -> None:
     import os
 
+    ref_root = ref_root or str(oracle.reference_root())
     os.environ["CELLFLOW_REFERENCE"] = ref_root
     if not oracle.build_ref(gpu=False):
         raise SystemExit("reference pieces not found")
@@ -162,7 +163,7 @@ if __name__ == "__main__":
         # add the mesh fixture to an existing manifest without rewriting the others
         import os
 
-        os.environ["CELLFLOW_REFERENCE"] = sys.argv[1] if len(sys.argv) > 2 else "/root/reference"
+        os.environ["CELLFLOW_REFERENCE"] = sys.argv[1] if len(sys.argv) > 2 else str(oracle.reference_root())
         if not oracle.build_ref(gpu=False):
             raise SystemExit("reference pieces not found")
         m = json.loads((HERE / "manifest.json").read_text())

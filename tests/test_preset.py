@@ -15,11 +15,13 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+import oracle
+
 from cellflow_gb300._lib import PRESET_BITS, CellFlowError
 from cellflow_gb300.world import SimulationParams, parse_preset
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-REFERENCE = Path(os.environ.get("CELLFLOW_REFERENCE", "/root/reference")) / "cuda-native"
+REFERENCE = oracle.reference_root() / "cuda-native"
 PRESETS = ["settings.json", "eater.json", "littlecells.json", "pulser.json"]
 
 F32 = np.float32
