@@ -747,7 +747,7 @@ ROLLOUT = {"rollout_n16k_k64": dict(n=16384, types=6, radius=0.1, steps=64, ever
                                     seed=0x5EED0005)}
 
 
-def run_rollout(args, rank, world, local, name="rollout_n16k_k64", steps=5, warmup=3):
+def run_rollout(args, rank, world, local, name="rollout_n16k_k64", steps=5, warmup=3, cpu_seconds=12.0):
     """rollout_n16k_k64: the differentiable rollout.  One bench step is one forward + backward
     pass of the K-step rollout with the soft radial distribution loss (cf_rollout_forward,
     cf_rdf, cf_rdf_backward, cf_rollout_backward); the plain step (cf_step, K steps) is timed
@@ -900,6 +900,13 @@ def run_rollout(args, rank, world, local, name="rollout_n16k_k64", steps=5, warm
                     "path": "pinned positions in, rollout + loss + adjoint, pinned position gradients out"},
             "gpu_launches": int(launches), "clocks": clk,
         }
+        if not args.no_cpu_baseline:
+            # the reference has no adjoint: its forward step on the rollout's world, for scale
+            v, kind, cores, desc = cpu_reference_sample(w, params, pos, types, table,
+                                                        np.zeros(T, np.float32), cpu_seconds)
+            line["cpu_baseline"] = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": kind,
+                                    "sample": desc + " (forward step only: the reference has no adjoint)",
+                                    "cpu_model": host_cpu_model()}
     sim.close()
     return line
 
@@ -1110,7 +1117,7 @@ def run_workload(args, rank, world, local, name, steps, warmup, cpu_seconds, ext
     if name in inputs.BATCHED:
         return run_batched(args, rank, world, local, name, steps, warmup, cpu_seconds)
     if name in ROLLOUT:
-        return run_rollout(args, rank, world, local, name, steps, warmup)
+        return run_rollout(args, rank, world, local, name, steps, warmup, cpu_seconds)
     return run_gb300(args, rank, world, local, name, steps, warmup, cpu_seconds, extras)
 
 

@@ -106,7 +106,7 @@ int main(int argc, char** argv)
                                          particleColors);
         for (auto& kv : buffers) cudaFree(kv.second);
 
-        std::printf("drop_in ok n=%d types=%d frames=%d line_vertices=%d triangle_vertices=%d pos_sum=%.9g "
+        std::printf("drop_in ok n=%d types=%d frames=%d line_vertices=%d triangle_vertices=%d pos_sum=%.17g "
                     "type_sum=%.0f extent=%g mapped=%d\n",
                     n, simulation->getNumParticleTypes(), f, gpuVertexCount, triangleVertexCount, pos_sum, type_sum,
                     maxUniverseSize, mapped);

@@ -106,12 +106,11 @@ def test_rollout_graphs_follow_scratch_reallocation(cflib):
     """The rollout's forward and backward run as cached CUDA graphs that read the
     cell-list scratch by address.  Proximity calls on much finer grids grow that
     scratch between rollouts of the same shape; the rollouts after them must not
-    replay a graph holding the freed buffers: their states and gradients equal a
-    run on the default stream, where no graph is used."""
+    replay a graph holding the freed buffers: their states and gradients equal
+    those of a world whose scratch never moved."""
     n, T, K, every = 3000, 4, 6, 3
     sim, params, *_ = make_world(n, T, 0.15, 21, 0.03)
     ref, *_ = make_world(n, T, 0.15, 21, 0.03)
-    ref.set_stream(None)
     start = sim.get_state()
     gx = dev4(np.ones((n, 3), np.float32))
 

@@ -124,8 +124,8 @@ def test_injected_cuda_error_is_reported_and_the_world_recovers(cflib, no_limits
 @pytest.mark.gpu
 def test_injection_skips_the_named_number_of_calls(cflib, no_limits):
     sim, params = world()
-    sim.set_stream(None)  # no graphs: one launch_step_force per step
-    assert cflib.cf_inject_cuda_error(b"launch_step_force", CUDA_ERROR_NOT_READY, 2) == 0
+    sim.simulate(params, 1)  # the step's graph is captured: from here one graph launch per step
+    assert cflib.cf_inject_cuda_error(b"cudaGraphLaunch", CUDA_ERROR_NOT_READY, 2) == 0
     sim.simulate(params, 2)
     assert cflib.cf_injection_pending() == 1
     with pytest.raises(CellFlowError):
