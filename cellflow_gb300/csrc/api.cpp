@@ -511,8 +511,14 @@ int prepare_step(cf_world* w, const cf_step_params* p, StepConsts* c)
     for (int a = 0; a < 3; a++) c->half[a] = c->ext[a] * 0.5f;
     c->inv_eff_uniform = 1.0f / c->eff_uniform;
     c->thr_lo_uniform = w->host_tables.threshold_lo[0];
-    c->variant = w->force_variant % kForceStages;
-    c->split = 1 << (w->force_variant / kForceStages);
+    if (w->force_variant < kForceStages * 3) {
+        c->variant = w->force_variant % kForceStages;
+        c->split = 1 << (w->force_variant / kForceStages);
+    } else {
+        // the balanced drain (staging 4): variants 12, 13, 14 for 1, 2, 4 warps per item
+        c->variant = kForceStages;
+        c->split = 1 << (w->force_variant - kForceStages * 3);
+    }
     c->thr_filter = filter_bound(thr_max, std::max(c->ext[0], std::max(c->ext[1], c->ext[2])));
     c->grid = choose_step_grid(c->ext, r_cut, kMaxCells);
     apply_worlds(c->grid, w->worlds);
@@ -1457,7 +1463,7 @@ int cf_set_force_variant(cf_world* w, int variant)
 {
     int rc = check_world(w);
     if (rc) return rc;
-    if (variant < 0 || variant >= CF_FORCE_VARIANTS) return fail(CF_ERR_INVALID, "force variant must be in [0, 12)");
+    if (variant < 0 || variant >= CF_FORCE_VARIANTS) return fail(CF_ERR_INVALID, "force variant must be in [0, 15)");
     w->force_variant = variant;
     return CF_OK;
 }

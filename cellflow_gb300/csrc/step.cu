@@ -128,16 +128,32 @@ struct PairScratch {
     uint32_t pairing[32];
 };
 struct NoScratch {};
+// Balanced drain: each lane's home and filter operands, group bitmap and hit
+// count for the batch, and the partial sums of the (lane, home) pieces of the
+// task line, at index lane + rank of the home among the homes with hits.
+struct BalScratch {
+    float4 home_h[32];
+    float4 home_m2[32];
+    uint32_t nzw[32];
+    int hits[32];
+    float4 part[64];
+};
 
 // Per-warp staging area, kStage candidates (a multiple of 32) per batch.
-template <int kStage, bool kPairs>
+// Drain modes: 0 one lane per home, 1 lanes paired (busiest with idlest),
+// 2 balanced (the batch's hits split evenly over the lanes).
+template <int kMode>
+using DrainScratch = typename std::conditional<kMode == 1, PairScratch,
+                                               typename std::conditional<kMode == 2, BalScratch, NoScratch>::type>::type;
+
+template <int kStage, int kMode>
 struct WarpSmem {
     float4 xy[kStage / 2];              // staged (x_a, x_b, y_a, y_b) of slots 2p, 2p+1
     float4 zc[kStage / 2];              // staged (z_a, z_b, |c_a|^2, |c_b|^2)
     uint32_t meta[kStage];              // sorted index | type << 27
     uint32_t mask[(kStage / 32) * 32];  // [group][lane]
     float origin[4];                    // the pass's staging origin (x, y, z)
-    typename std::conditional<kPairs, PairScratch, NoScratch>::type pr;
+    DrainScratch<kMode> pr;
 };
 
 // Named barrier of the warps sharing an item: id 1 + slot (slot < kWarps),
@@ -255,7 +271,7 @@ __device__ __forceinline__ void staged_xyz(const float* xyf, const float* zcf, i
     z = zcf[pb];
 }
 
-template <int kStage, int kMinBlocks, bool kPairs, bool kGeneric, bool kUniformR>
+template <int kStage, int kMinBlocks, int kMode, bool kGeneric, bool kUniformR>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
     step_force_kernel(StepConsts c, const PairTables* __restrict__ tables, const float4* __restrict__ pos_sorted,
                       const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ vals_sorted,
@@ -273,7 +289,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     // force coefficients, compact T-stride: one copy per block for a single
     // world, one per warp (filled once its item's world is known) for a batch
     const bool one_world = c.grid.worlds == 1;
-    float2* coef_base = reinterpret_cast<float2*>(s_dyn + sizeof(WarpSmem<kStage, kPairs>) * kWarps);
+    float2* coef_base = reinterpret_cast<float2*>(s_dyn + sizeof(WarpSmem<kStage, kMode>) * kWarps);
     if (!kUniformR) {
         for (int e = threadIdx.x; e < T * T; e += kThreads) {
             const int a = e / T, b = e - a * T;
@@ -298,9 +314,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     // pairs per drain trip: two side by side where the register budget allows,
     // three with lane pairing (more of the lanes stay busy, so more independent
     // work per trip pays there; it does not without pairing)
-    constexpr int kPer = kMinBlocks >= 8 ? 1 : (kPairs && !kGeneric ? 3 : 2);
-    // lane pairing in the drain (regular grids)
-    constexpr bool kBalance = kPairs && !kGeneric;
+    constexpr int kPer = kMinBlocks >= 8 ? 1 : (kMode != 0 && !kGeneric ? 3 : 2);
+    // lane pairing or the balanced drain (regular grids)
+    constexpr bool kBalance = kMode == 1 && !kGeneric;
+    constexpr bool kBal = kMode == 2 && !kGeneric;
 
     // c.split warps (1, 2 or 4) share an item, each taking an equal share of its
     // candidates; part 0 adds the others' partial sums and integrates
@@ -309,7 +326,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const int part = warp & (split - 1);
     const int item = blockIdx.x * (kWarps / split) + warp / split;
     if (item >= *n_items) return;  // the item's other warps leave too: no barrier is pending
-    using Smem = WarpSmem<kStage, kPairs>;
+    using Smem = WarpSmem<kStage, kMode>;
     Smem& w = reinterpret_cast<Smem*>(s_dyn)[warp];
     float2* wcoef = coef_base + (one_world ? 0 : warp * T * T);
     const float* xyf = reinterpret_cast<const float*>(w.xy);
@@ -386,7 +403,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 w.origin[1] = oy;
                 w.origin[2] = oz;
             }
-            if constexpr (kBalance) {
+            if constexpr (kBalance || kBal) {
                 w.pr.home_h[lane] = L.h;
                 w.pr.home_m2[lane] = make_float4(H.m2x.x, H.m2y.x, H.m2z.x, 0.0f);
             }
@@ -551,6 +568,156 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             // the top part of its partner's hits with its partner's home, accumulating them
             // apart; the partner adds that partial after the trips.  Each pair's work is then
             // about half its total.
+            if constexpr (kBal) {
+                // ---- balanced drain: the batch's H hits, home by home in lane order, form a
+                // task line; lane l takes tasks [l H / 32, (l + 1) H / 32), walking each home's
+                // set bits with that home's position (a new home starts a new trip), and
+                // writes the partial sums of each (lane, home) piece to part[lane + rank of
+                // the home]; each home then adds its pieces in lane order (deterministic).
+                w.pr.nzw[lane] = nz;
+                w.pr.hits[lane] = hits;
+                int pre = hits;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, pre, o);
+                    if (lane >= o) pre += v;
+                }
+                const int H_all = __shfl_sync(0xffffffffu, pre, 31);
+                pre -= hits;  // exclusive prefix: where this lane's home starts on the task line
+                const uint32_t has = __ballot_sync(0xffffffffu, hits > 0);
+                const int t0 = (lane * H_all) >> 5, t1 = ((lane + 1) * H_all) >> 5;
+                int left = t1 - t0;
+                // the home of task t0: the last home whose start is <= t0 (a home with hits)
+                int hm = 0;
+#pragma unroll
+                for (int step = 16; step >= 1; step >>= 1) {
+                    const int cand = hm + step;
+                    if (__shfl_sync(0xffffffffu, pre, cand) <= t0) hm = cand;
+                }
+                const int rank0 = t0 - __shfl_sync(0xffffffffu, pre, hm);
+                __syncwarp();
+                uint32_t m = 0u;
+                int gi = 0, inh = 0;
+                if (left > 0) {
+                    // skip the first rank0 set bits of home hm
+                    int r = rank0;
+                    nz = w.pr.nzw[hm];
+                    for (;;) {
+                        gi = __ffs(nz) - 1;
+                        m = w.mask[gi * 32 + hm];
+                        const int cnt = __popc(m);
+                        if (r < cnt) break;
+                        r -= cnt;
+                        nz &= nz - 1u;
+                    }
+                    for (; r > 0; r--) m &= m - 1u;
+                    inh = min(left, w.pr.hits[hm] - rank0);
+                    const float4 ph = w.pr.home_h[hm];
+                    const float4 pm = w.pr.home_m2[hm];
+                    L.h = ph;
+                    L.tp = __float_as_uint(ph.w) & kTypeMask;
+                    H.m2x.x = pm.x;
+                    H.m2y.x = pm.y;
+                    H.m2z.x = pm.z;
+                }
+                const bool worked = left > 0;
+                // running sums of this lane's own home stay in (sx, sy, sz, sc); L accumulates pieces
+                const float sx = L.fx, sy = L.fy, sz = L.fz;
+                const int sc = L.count;
+                L.fx = L.fy = L.fz = 0.0f;
+                L.count = 0;
+                while (__any_sync(0xffffffffu, left > 0)) {
+                    if (left > 0 && inh == 0) {
+                        // this home's tasks are done: its piece goes to part[], the next home starts
+                        w.pr.part[lane + __popc(has & ((1u << hm) - 1u))] =
+                            make_float4(L.fx, L.fy, L.fz, __int_as_float(L.count));
+                        L.fx = L.fy = L.fz = 0.0f;
+                        L.count = 0;
+                        hm = __ffs(has & (0xfffffffeu << hm)) - 1;
+                        nz = w.pr.nzw[hm];
+                        gi = __ffs(nz) - 1;
+                        m = w.mask[gi * 32 + hm];
+                        inh = min(left, w.pr.hits[hm]);
+                        const float4 ph = w.pr.home_h[hm];
+                        const float4 pm = w.pr.home_m2[hm];
+                        L.h = ph;
+                        L.tp = __float_as_uint(ph.w) & kTypeMask;
+                        H.m2x.x = pm.x;
+                        H.m2y.x = pm.y;
+                        H.m2z.x = pm.z;
+                    }
+                    const int nq = min(kPer, inh);
+                    int slot[kPer];
+                    bool valid[kPer];
+#pragma unroll
+                    for (int q = 0; q < kPer; q++) {
+                        valid[q] = q < nq;
+                        if (valid[q] && m == 0u) {
+                            nz &= nz - 1u;
+                            gi = __ffs(nz) - 1;
+                            m = w.mask[gi * 32 + hm];
+                        }
+                        slot[q] = valid[q] ? gi * 32 + (__ffs(m) - 1) : 0;
+                        if (valid[q]) m &= m - 1u;
+                    }
+                    float dx[kPer], dy[kPer], dz[kPer], d2[kPer], wgt[kPer];
+                    uint32_t meta[kPer];
+                    bool inter[kPer];
+#pragma unroll
+                    for (int q = 0; q < kPer; q++) {
+                        float x, y, z;
+                        staged_xyz(xyf, zcf, slot[q], x, y, z);
+                        meta[q] = w.meta[slot[q]];
+                        inter[q] = valid[q] && pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta[q],
+                                                                              pos_sorted, tb, dx[q], dy[q], dz[q],
+                                                                              d2[q]);
+                    }
+#pragma unroll
+                    for (int q = 0; q < kPer; q++) wgt[q] = pair_weight<kUniformR>(d2[q], meta[q], L, tb, c1u);
+#pragma unroll
+                    for (int q = 0; q < kPer; q++) {
+                        if (inter[q]) {
+                            L.count++;
+                            L.fx = fmaf(dx[q], wgt[q], L.fx);
+                            L.fy = fmaf(dy[q], wgt[q], L.fy);
+                            L.fz = fmaf(dz[q], wgt[q], L.fz);
+                        }
+                    }
+                    inh -= nq;
+                    left -= nq;
+                }
+                if (worked)
+                    w.pr.part[lane + __popc(has & ((1u << hm) - 1u))] =
+                        make_float4(L.fx, L.fy, L.fz, __int_as_float(L.count));
+                __syncwarp();
+                // each home adds its pieces in lane order; back to the lane's own home
+                L.fx = sx;
+                L.fy = sy;
+                L.fz = sz;
+                L.count = sc;
+                if (hits > 0) {
+                    // lanes la..lb hold the home's tasks (those with an empty range, when the
+                    // batch has fewer hits than lanes, hold none)
+                    const int rk = __popc(has & ((1u << lane) - 1u));
+                    const int la = (32 * (pre + 1) - 1) / H_all;
+                    const int lb = (32 * (pre + hits) - 1) / H_all;
+                    for (int l2 = la; l2 <= lb; l2++) {
+                        if (((l2 + 1) * H_all) >> 5 == (l2 * H_all) >> 5) continue;
+                        const float4 v = w.pr.part[l2 + rk];
+                        L.fx += v.x;
+                        L.fy += v.y;
+                        L.fz += v.z;
+                        L.count += __float_as_int(v.w);
+                    }
+                }
+                const float4 oh = w.pr.home_h[lane];
+                const float4 om = w.pr.home_m2[lane];
+                L.h = oh;
+                L.tp = __float_as_uint(oh.w) & kTypeMask;
+                H.m2x.x = om.x;
+                H.m2y.x = om.y;
+                H.m2z.x = om.z;
+            } else {
             int upto = hits;         // pair indices below upto are valid in the current phase
             int work = hits;         // pairs this lane walks in the batch
             int switch_trip = -1;    // trip at which a light lane turns to its partner's hits
@@ -692,6 +859,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     L.count += pc;
                 }
             }
+            }
             __syncwarp();
         }
     }
@@ -771,14 +939,14 @@ __global__ void __launch_bounds__(1024)
     if (tid == 1023) *n_items = (int)s_chunk[1023];
 }
 
-template <int S, int B, bool P, bool G, bool U>
+template <int S, int B, int P, bool G, bool U>
 cudaError_t configure_one()
 {
     return cudaFuncSetAttribute(step_force_kernel<S, B, P, G, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)((sizeof(WarpSmem<S, P>) + sizeof(float2) * kTableSize) * kWarps));
 }
 
-template <int S, int B, bool P>
+template <int S, int B, int P>
 cudaError_t configure_variant()
 {
     cudaError_t e = configure_one<S, B, P, false, false>();
@@ -790,7 +958,7 @@ cudaError_t configure_variant()
 
 // Variant S = staged candidates per batch, B = resident blocks per SM the
 // register budget is sized for, P = lanes paired in the drain.
-template <int S, int B, bool P>
+template <int S, int B, int P>
 cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const float4* pos_sorted,
                            const uint32_t* keys_sorted, const uint32_t* vals_sorted, const uint32_t* cell_off,
                            const Item* items, const int* n_items, int blocks, float4* pos, float4* vel, float4* acc,
@@ -837,10 +1005,11 @@ cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, Ite
 // stream capture).
 cudaError_t configure_step_force()
 {
-    cudaError_t e = configure_variant<256, 8, false>();
-    if (e == cudaSuccess) e = configure_variant<256, 6, false>();
-    if (e == cudaSuccess) e = configure_variant<256, 6, true>();
-    if (e == cudaSuccess) e = configure_variant<384, 6, false>();
+    cudaError_t e = configure_variant<256, 8, 0>();
+    if (e == cudaSuccess) e = configure_variant<256, 6, 0>();
+    if (e == cudaSuccess) e = configure_variant<256, 6, 1>();
+    if (e == cudaSuccess) e = configure_variant<384, 6, 0>();
+    if (e == cudaSuccess) e = configure_variant<256, 6, 2>();
     return e;
 }
 
@@ -854,16 +1023,19 @@ cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, con
     const int blocks = (int)(((long long)max_items * c.split + kWarps - 1) / kWarps);
     switch (c.variant) {
     case 1:
-        return launch_variant<256, 6, false>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+        return launch_variant<256, 6, 0>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
                                       blocks, pos, vel, acc, counts, st);
     case 2:
-        return launch_variant<256, 6, true>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+        return launch_variant<256, 6, 1>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
                                       blocks, pos, vel, acc, counts, st);
+    case 4:
+        return launch_variant<256, 6, 2>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+                                         blocks, pos, vel, acc, counts, st);
     case 3:
-        return launch_variant<384, 6, false>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+        return launch_variant<384, 6, 0>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
                                       blocks, pos, vel, acc, counts, st);
     default:
-        return launch_variant<256, 8, false>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
+        return launch_variant<256, 8, 0>(c, tables, pos_sorted, keys_sorted, vals_sorted, cell_off, items, n_items,
                                       blocks, pos, vel, acc, counts, st);
     }
 }

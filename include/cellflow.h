@@ -243,10 +243,14 @@ int cf_step_host(cf_world* w, const cf_step_params* p, const cf_particle* in, cf
  * sorted hit counts); 3 = 384 staged, 6 blocks per SM.  v / 4 picks the warps
  * per 32-particle item: 1, 2 or 4 (each warp takes an equal share of the
  * item's candidates; more warps for worlds too small to fill the GPU).
+ * Variants 12, 13 and 14 use the balanced drain (256 staged, 6 blocks per
+ * SM) with 1, 2 or 4 warps per item: a batch's hits, home by home, are split
+ * into 32 equal ranges, one per lane, and each home adds the partial sums of
+ * its pieces in lane order.
  * Results are bit-identical across stagings 0, 1 and 3; with lane pairing,
- * and with 2 or 4 warps, partial sums are added in a fixed order, which
- * differs from the single-lane order by rounding only. */
-#define CF_FORCE_VARIANTS 12
+ * the balanced drain, and 2 or 4 warps, partial sums are added in a fixed
+ * order, which differs from the single-lane order by rounding only. */
+#define CF_FORCE_VARIANTS 15
 /* Autotuner of the step (no counterpart in the reference): runs `steps`
  * trial steps with each force-kernel variant, restores the particle state,
  * keeps the fastest variant for later steps and returns it in

@@ -108,7 +108,7 @@ def test_every_particle_in_one_cell(cflib):
     table = rng.normal(0, 0.5, (T, T)).astype(np.float32)
     rec, counts = step_vs_oracle(pos, types, table, params, label="one cell")
     assert counts.min() == n - 1
-    for variant in (2, 5, 11):
+    for variant in (2, 5, 11, 12, 14):
         step_vs_oracle(pos, types, table, params, variant=variant, label=f"one cell, variant {variant}")
 
 
@@ -147,7 +147,7 @@ def test_rows_of_4096_cells(cflib):
     assert np.abs(rec["acc"][sel] - ao[sel]).max() <= 1e-5 * scale
 
 
-@pytest.mark.parametrize("variant", range(12))
+@pytest.mark.parametrize("variant", range(15))
 def test_single_item_world_under_every_variant(cflib, variant):
     """20 particles in one cell of a 6-cell grid: one item, so with 2 or 4 warps per item some
     warps have few or no candidates."""
@@ -158,11 +158,12 @@ def test_single_item_world_under_every_variant(cflib, variant):
     assert counts.min() == 19
 
 
-@pytest.mark.parametrize("variant", [1, 2, 6, 10])
+@pytest.mark.parametrize("variant", [1, 2, 6, 10, 12, 13, 14])
 def test_skewed_occupancy_under_lane_pairing(cflib, variant):
     """Dense Gaussian blobs (hundreds of neighbours next to a few): the lanes of an item have
     very uneven hit counts, so the lane-paired drain (stagings 2: variants 2, 6, 10) hands
-    large parts of busy lanes' hits to idle ones; counts stay bit-exact and forces within
+    large parts of busy lanes' hits to idle ones, and the balanced drain (variants 12-14)
+    splits every batch's hits evenly over the lanes; counts stay bit-exact and forces within
     the step tolerance, as with the unpaired staging (variant 1)."""
     n, T = 12000, 5
     pos = inputs.blob_positions(n, 6, 0.04, 0x5EED0031)

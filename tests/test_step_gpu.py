@@ -169,21 +169,23 @@ def test_autotune_keeps_state_and_results(cflib):
     sim, pos, types, table, radio = make_world(w)
     before = sim.get_state()
     chosen = sim.autotune(params, 2)
-    assert chosen in range(12)
+    assert chosen in range(15)
     after = sim.get_state()
     for a, b in zip(before, after):
         assert np.array_equal(a, b)
     sim.close()
     results, counts = {}, {}
-    for variant in range(12):
+    for variant in range(15):
         s, *_ = make_world(w, pos, types, table, radio)
         s.set_force_variant(variant)
         s.simulate(params, 1)
         results[variant] = s.getParticleData()
         counts[variant] = s.getNeighborCounts()
         s.close()
-    for variant in range(12):
-        same_split = variant - variant % 4 + (2 if variant % 4 == 2 else 0)
+    for variant in range(15):
+        # the unpaired stagings 0, 1, 3 of one split give identical results; the paired (2) and
+        # balanced (12-14) drains add partial sums in their own fixed order
+        same_split = variant if variant >= 12 else variant - variant % 4 + (2 if variant % 4 == 2 else 0)
         for f in ("pos", "vel", "acc"):
             assert np.array_equal(results[same_split][f], results[variant][f]), (variant, f)
         assert np.array_equal(counts[0], counts[variant]), variant
@@ -191,7 +193,7 @@ def test_autotune_keeps_state_and_results(cflib):
         assert np.abs(results[0]["acc"] - results[variant]["acc"]).max() <= 1e-6 * scale, variant
     s, *_ = make_world(w, pos, types, table, radio)
     with pytest.raises(CellFlowError):
-        s.set_force_variant(12)
+        s.set_force_variant(15)
     s.close()
 
 
