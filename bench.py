@@ -399,9 +399,10 @@ def run_gb300(args, rank, world, local, name, steps, warmup, cpu_seconds, extras
 
     # ---- work counters: replay the same K steps from the same state, untimed
     sim.set_state(*state0)
-    c27_total, inter_total = 0, 0
+    c27_total, inter_total, tested_total = 0, 0, 0
     for _ in range(steps):
         c27, _ = sim.work_counters(params)
+        tested_total += sim.force_work(params)[1]
         sim.simulate(params, 1)
         _, inter = sim.work_counters(params)
         c27_total += c27
@@ -489,6 +490,9 @@ def run_gb300(args, rank, world, local, name, steps, warmup, cpu_seconds, extras
                 "work_model": "9*C27 + 17*I + 25*N flops per step",
                 "c27_per_particle_step": c27_total / (w.n * steps),
                 "interacting_per_particle_step": inter_total / (w.n * steps),
+                "tested_per_particle_step": tested_total / (w.n * steps),
+                "tested_note": "candidate tests of the force kernel's filter per particle (cf_force_work): the "
+                               "union of each 32-particle item's stencils, against the canonical C27",
                 "traffic": (profiled_traffic(w.name) or {}).get("bytes_per_launch"),
                 "traffic_unit": "bytes per launch (one ncu capture of this workload's force kernel)",
                 "traffic_source": (profiled_traffic(w.name) or {}).get("source"),

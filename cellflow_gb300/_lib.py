@@ -190,6 +190,7 @@ _SIGNATURES = {
         [_W, _P(StepParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
     ),
     "cf_work_counters": (C.c_int, [_W, _P(StepParams), _P(C.c_uint64), _P(C.c_uint64)]),
+    "cf_force_work": (C.c_int, [_W, _P(StepParams), _P(C.c_uint64), _P(C.c_uint64)]),
     "cf_proximity_edges": (C.c_int, [_W, C.c_float, C.c_int, C.c_void_p, C.c_int, _P(C.c_int)]),
     "cf_proximity_vertices_device": (
         C.c_int,

@@ -1642,6 +1642,31 @@ int cf_debug_cell_list(cf_world* w, const cf_step_params* p, uint32_t* cell_of, 
     return CF_OK;
 }
 
+int cf_force_work(cf_world* w, const cf_step_params* p, uint64_t* staged, uint64_t* tested)
+{
+    int rc = check_world(w);
+    if (rc) return rc;
+    StepConsts c;
+    rc = prepare_step(w, p, &c);
+    if (!rc) rc = ensure_cells(w, c.grid.cells);
+    if (!rc) rc = ensure_plan(w, c.grid);
+    if (!rc) rc = ensure_offsets(w, c.grid.cells);
+    if (rc) return rc;
+    int which = 0;
+    rc = enqueue_cell_list(w, c, &which);
+    if (rc) return rc;
+    Scratch& s = w->s;
+    CF_CUDA(launch_force_work(c, s.keys[which], s.cell_off, s.items, s.n_items, max_step_items(w->n, c.grid),
+                              s.counters, w->stream));
+    unsigned long long host[2] = {0, 0};
+    CF_CUDA(cudaMemcpyAsync(host, s.counters, sizeof(host), cudaMemcpyDeviceToHost, w->stream));
+    rc = sync_and_check(w);
+    if (rc) return rc;
+    if (staged) *staged = host[0];
+    if (tested) *tested = host[1];
+    return CF_OK;
+}
+
 int cf_work_counters(cf_world* w, const cf_step_params* p, uint64_t* c27, uint64_t* interacting)
 {
     int rc = check_world(w);

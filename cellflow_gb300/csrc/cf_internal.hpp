@@ -315,6 +315,9 @@ cudaError_t launch_step_force(const StepConsts& c, const PairTables* tables, con
                               const Item* items, const int* n_items, int max_items, float4* pos, float4* vel,
                               float4* acc, int* counts, cudaStream_t st);
 // Row-aligned items of at most 32 sorted particles (one cell row each).
+cudaError_t launch_force_work(const StepConsts& c, const uint32_t* keys_sorted, const uint32_t* cell_off,
+                              const Item* items, const int* n_items, int max_items, unsigned long long* out,
+                              cudaStream_t st);
 cudaError_t launch_step_plan(const uint32_t* cell_off, int n, const Grid& g, Item* items, int* n_items,
                              cudaStream_t st);
 int max_step_items(int n, const Grid& g);

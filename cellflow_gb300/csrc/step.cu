@@ -127,7 +127,9 @@ struct PairScratch {
     uint32_t nzw[32];
     uint32_t pairing[32];
 };
-struct NoScratch {};
+struct NoScratch {
+    float4 home_h[32];
+};
 // Balanced drain: each lane's home and filter operands, group bitmap and hit
 // count for the batch, and the partial sums of the (lane, home) pieces of the
 // task line, at index lane + rank of the home among the homes with hits.
@@ -140,6 +142,13 @@ struct BalScratch {
 };
 
 // Per-warp staging area, kStage candidates (a multiple of 32) per batch.
+// Band pairs of a batch: filter hits whose staged distance is within rounding
+// of the threshold.  The drain lists them (a rarely taken, warp-uniform branch)
+// and they are resolved after it with the reference's exact test, so the
+// drain's trips carry no exact-test code; a batch with more than kBandCap of
+// them re-walks its homes' hits instead.
+constexpr int kBandCap = 64;
+
 // Drain modes: 0 one lane per home, 1 lanes paired (busiest with idlest),
 // 2 balanced (the batch's hits split evenly over the lanes).
 template <int kMode>
@@ -153,6 +162,8 @@ struct WarpSmem {
     uint32_t meta[kStage];              // sorted index | type << 27
     uint32_t mask[(kStage / 32) * 32];  // [group][lane]
     float origin[4];                    // the pass's staging origin (x, y, z)
+    uint32_t band[kBandCap];            // band pairs of the batch: slot | home lane << 16
+    float4 band_acc[32];                // per home: force and count of its band pairs, all batches
     DrainScratch<kMode> pr;
 };
 
@@ -219,16 +230,26 @@ __device__ __forceinline__ void staged_delta(const StepConsts& c, float cx, floa
 // fallback.  Returns the staged displacement and its contracted d^2.
 // `origin` is the pass's staging origin (unused on generic grids).
 template <bool kGeneric, bool kUniformR>
+__device__ __forceinline__ bool pair_certain(const StepConsts& c, const Lane& L, const HomeOps& H, float cx, float cy,
+                                             float cz, uint32_t meta, const Tables& tb, float& dx, float& dy,
+                                             float& dz, float& d2)
+{
+    staged_delta<kGeneric>(c, cx, cy, cz, L.h, H, dx, dy, dz);
+    d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const uint32_t pair = L.tp * kTableStride + (meta >> kTypeShift);
+    return d2 < (kUniformR ? c.thr_lo_uniform : tb.thr_lo[pair]);
+}
+
+// The full test: the certain-interaction bound, then the reference's exact test
+// for a pair within rounding of the threshold.
+template <bool kGeneric, bool kUniformR>
 __device__ __forceinline__ bool pair_test(const StepConsts& c, const Lane& L, const HomeOps& H,
                                           const float* origin, float cx, float cy, float cz, uint32_t meta,
                                           const float4* __restrict__ pos_sorted, const Tables& tb, float& dx,
                                           float& dy, float& dz, float& d2)
 {
-    staged_delta<kGeneric>(c, cx, cy, cz, L.h, H, dx, dy, dz);
-    d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    const uint32_t other = meta >> kTypeShift;
-    const uint32_t pair = L.tp * kTableStride + other;
-    bool inter = d2 < (kUniformR ? c.thr_lo_uniform : tb.thr_lo[pair]);
+    const uint32_t pair = L.tp * kTableStride + (meta >> kTypeShift);
+    bool inter = pair_certain<kGeneric, kUniformR>(c, L, H, cx, cy, cz, meta, tb, dx, dy, dz, d2);
     if (!inter) {
         // within rounding of the threshold: the reference's exact test
         const float4 o = pos_sorted[meta & kIndexMask];
@@ -339,6 +360,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     L.tp = __float_as_uint(L.h.w) & kTypeMask;
     L.fx = L.fy = L.fz = 0.0f;
     L.count = 0;
+    w.pr.home_h[lane] = L.h;
+    w.band_acc[lane] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 
     // cell coordinates inside the item's world (items never straddle worlds or rows)
     const int mx = c.grid.m[0], my = c.grid.m[1], mz = c.grid.m[2];
@@ -403,10 +426,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 w.origin[1] = oy;
                 w.origin[2] = oz;
             }
-            if constexpr (kBalance || kBal) {
-                w.pr.home_h[lane] = L.h;
-                w.pr.home_m2[lane] = make_float4(H.m2x.x, H.m2y.x, H.m2z.x, 0.0f);
-            }
+            if constexpr (kBalance || kBal) w.pr.home_m2[lane] = make_float4(H.m2x.x, H.m2y.x, H.m2z.x, 0.0f);
         } else {
             H.m2x = H.m2y = H.m2z = H.k = make_float2(0.0f, 0.0f);
         }
@@ -568,6 +588,22 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             // the top part of its partner's hits with its partner's home, accumulating them
             // apart; the partner adds that partial after the trips.  Each pair's work is then
             // about half its total.
+            const uint32_t nz_own = nz;  // this lane's own groups with hits (the overflow re-walk)
+            int nband = 0;               // band pairs listed in this batch (warp-uniform)
+            bool band_overflow = false;
+            // list the band pairs of one trip (bit q of `band`: pair q of this lane)
+            auto list_band = [&](uint32_t band, const int* slot, int home) {
+                if (!__any_sync(0xffffffffu, band != 0u)) return;
+#pragma unroll
+                for (int q = 0; q < kPer; q++) {
+                    const bool mine = (band >> q) & 1u;
+                    const uint32_t b = __ballot_sync(0xffffffffu, mine);
+                    if (nband + __popc(b) > kBandCap) band_overflow = true;
+                    if (!band_overflow && mine)
+                        w.band[nband + __popc(b & ((1u << lane) - 1u))] = (uint32_t)slot[q] | ((uint32_t)home << 16);
+                    if (!band_overflow) nband += __popc(b);
+                }
+            };
             if constexpr (kBal) {
                 // ---- balanced drain: the batch's H hits, home by home in lane order, form a
                 // task line; lane l takes tasks [l H / 32, (l + 1) H / 32), walking each home's
@@ -649,6 +685,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     const int nq = min(kPer, inh);
                     int slot[kPer];
                     bool valid[kPer];
+                    uint32_t band = 0u;
 #pragma unroll
                     for (int q = 0; q < kPer; q++) {
                         valid[q] = q < nq;
@@ -668,9 +705,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         float x, y, z;
                         staged_xyz(xyf, zcf, slot[q], x, y, z);
                         meta[q] = w.meta[slot[q]];
-                        inter[q] = valid[q] && pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta[q],
-                                                                              pos_sorted, tb, dx[q], dy[q], dz[q],
-                                                                              d2[q]);
+                        const bool certain = pair_certain<kGeneric, kUniformR>(c, L, H, x, y, z, meta[q], tb, dx[q],
+                                                                               dy[q], dz[q], d2[q]);
+                        inter[q] = valid[q] && certain;
+                        band |= (valid[q] && !certain ? 1u : 0u) << q;
                     }
 #pragma unroll
                     for (int q = 0; q < kPer; q++) wgt[q] = pair_weight<kUniformR>(d2[q], meta[q], L, tb, c1u);
@@ -685,6 +723,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     }
                     inh -= nq;
                     left -= nq;
+                    list_band(band, slot, hm);
                 }
                 if (worked)
                     w.pr.part[lane + __popc(has & ((1u << hm) - 1u))] =
@@ -793,8 +832,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         upto = kPer * it + fw;
                     }
                 }
+                int slot[kPer];
+                uint32_t band = 0u;
                 if (kPer * it < upto) {
-                    int slot[kPer];
                     bool valid[kPer];
 #pragma unroll
                     for (int q = 0; q < kPer; q++) {
@@ -815,9 +855,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         float x, y, z;
                         staged_xyz(xyf, zcf, slot[q], x, y, z);
                         meta[q] = w.meta[slot[q]];
-                        inter[q] = pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta[q], pos_sorted, tb,
-                                                                  dx[q], dy[q], dz[q], d2[q]) &&
-                                   valid[q];
+                        const bool certain = pair_certain<kGeneric, kUniformR>(c, L, H, x, y, z, meta[q], tb, dx[q],
+                                                                               dy[q], dz[q], d2[q]);
+                        inter[q] = certain && valid[q];
+                        band |= (!certain && valid[q] ? 1u : 0u) << q;
                     }
 #pragma unroll
                     for (int q = 0; q < kPer; q++) wgt[q] = pair_weight<kUniformR>(d2[q], meta[q], L, tb, c1u);
@@ -831,6 +872,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         }
                     }
                 }
+                list_band(band, slot, src);
             }
             if constexpr (kBalance) {
                 // a light lane that switched holds its partner's partial: hand it over and
@@ -860,8 +902,92 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 }
             }
             }
+            // ---- band pairs, every lane back on its own home: listed ones resolved in
+            // parallel (lane e takes entry e) and added by their homes in list order; after
+            // an overflow, every lane re-walks its own hits of the batch for them instead.
+            // They go to the home's band accumulator, in the order the homes' hits are
+            // concatenated whatever the batch size, and join its sums once, after the last
+            // batch
+            __syncwarp();
+            if (band_overflow) {
+                uint32_t zz = nz_own;
+                while (zz) {
+                    const int g = __ffs(zz) - 1;
+                    zz &= zz - 1u;
+                    uint32_t mm = w.mask[g * 32 + lane];
+                    while (mm) {
+                        const int slot = g * 32 + (__ffs(mm) - 1);
+                        mm &= mm - 1u;
+                        float x, y, z, dx, dy, dz, d2;
+                        staged_xyz(xyf, zcf, slot, x, y, z);
+                        const uint32_t meta = w.meta[slot];
+                        if (pair_certain<kGeneric, kUniformR>(c, L, H, x, y, z, meta, tb, dx, dy, dz, d2)) continue;
+                        if (pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta, pos_sorted, tb, dx, dy,
+                                                           dz, d2)) {
+                            const float wgt = pair_weight<kUniformR>(d2, meta, L, tb, c1u);
+                            float4 a = w.band_acc[lane];
+                            a.x = fmaf(dx, wgt, a.x);
+                            a.y = fmaf(dy, wgt, a.y);
+                            a.z = fmaf(dz, wgt, a.z);
+                            a.w += 1.0f;
+                            w.band_acc[lane] = a;
+                        }
+                    }
+                }
+            } else {
+                for (int e0 = 0; e0 < nband; e0 += 32) {
+                    float bx = 0.0f, by = 0.0f, bz = 0.0f;
+                    int bc = 0, bhome = -1;
+                    if (e0 + lane < nband) {
+                        const uint32_t ent = w.band[e0 + lane];
+                        const int slot = (int)(ent & 0xffffu);
+                        bhome = (int)(ent >> 16);
+                        Lane Lb;
+                        Lb.h = w.pr.home_h[bhome];
+                        Lb.tp = __float_as_uint(Lb.h.w) & kTypeMask;
+                        HomeOps Hb;
+                        Hb.m2x = make_float2(-2.0f * (Lb.h.x - w.origin[0]), 0.0f);
+                        Hb.m2y = make_float2(-2.0f * (Lb.h.y - w.origin[1]), 0.0f);
+                        Hb.m2z = make_float2(-2.0f * (Lb.h.z - w.origin[2]), 0.0f);
+                        float x, y, z, dx, dy, dz, d2;
+                        staged_xyz(xyf, zcf, slot, x, y, z);
+                        const uint32_t meta = w.meta[slot];
+                        if (pair_test<kGeneric, kUniformR>(c, Lb, Hb, w.origin, x, y, z, meta, pos_sorted, tb, dx, dy,
+                                                           dz, d2)) {
+                            const float wgt = pair_weight<kUniformR>(d2, meta, Lb, tb, c1u);
+                            bx = dx * wgt;
+                            by = dy * wgt;
+                            bz = dz * wgt;
+                            bc = 1;
+                        }
+                    }
+                    const int cnt = min(32, nband - e0);
+                    for (int e = 0; e < cnt; e++) {
+                        const int hme = __shfl_sync(0xffffffffu, bhome, e);
+                        const float ex = __shfl_sync(0xffffffffu, bx, e), ey = __shfl_sync(0xffffffffu, by, e),
+                                    ez = __shfl_sync(0xffffffffu, bz, e);
+                        const int ec = __shfl_sync(0xffffffffu, bc, e);
+                        if (lane == hme) {
+                            float4 a = w.band_acc[lane];
+                            a.x += ex;
+                            a.y += ey;
+                            a.z += ez;
+                            a.w += (float)ec;
+                            w.band_acc[lane] = a;
+                        }
+                    }
+                }
+            }
             __syncwarp();
         }
+    }
+    {
+        __syncwarp();
+        const float4 a = w.band_acc[lane];
+        L.fx += a.x;
+        L.fy += a.y;
+        L.fz += a.z;
+        L.count += (int)a.w;
     }
     if (split > 1) {
         // the item's warps meet at a named barrier (id 1 + item slot, 32 * split threads);
@@ -903,6 +1029,74 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     vel[i] = make_float4(vx, vy, vz, 0.0f);
     acc[i] = make_float4(fx, fy, fz, 0.0f);
     counts[i] = L.count;
+}
+
+// The filter's work of one step, from the cell list alone: per item and pass
+// the candidates staged (the union of its homes' stencils, as the force
+// kernel concatenates them) and the tests of them by the item's particles.
+// One thread per item; out[0] += staged, out[1] += staged * particles.
+__global__ void __launch_bounds__(256)
+    force_work_kernel(StepConsts c, const uint32_t* __restrict__ keys_sorted, const uint32_t* __restrict__ cell_off,
+                      const Item* __restrict__ items, const int* __restrict__ n_items,
+                      unsigned long long* __restrict__ out)
+{
+    const int k = blockIdx.x * 256 + threadIdx.x;
+    unsigned long long staged = 0, tested = 0;
+    if (k < *n_items) {
+        const Item it = items[k];
+        const int mx = c.grid.m[0], my = c.grid.m[1], mz = c.grid.m[2];
+        const uint32_t world_base = (uint32_t)it.world * (uint32_t)c.grid.cells_w;
+        const int yc = it.yz & 0xffff, zc = it.yz >> 16;
+        const uint32_t row_base = world_base + (uint32_t)((zc * my + yc) * mx);
+        const int x0 = (int)(keys_sorted[it.first] - row_base);
+        const int x1 = (int)(keys_sorted[it.first + it.count - 1] - row_base);
+        const bool generic = c.grid.generic != 0;
+        const int width = generic ? mx : (mx - 2);
+        const int passes = generic ? 1 : (x1 - x0 + width) / width;
+        const int ny = my > 1 ? 3 : 1, nz = mz > 1 ? 3 : 1;
+        for (int pass = 0; pass < passes; pass++) {
+            const int px0 = generic ? x0 : x0 + pass * width;
+            const int px1 = generic ? x1 : min(x1, px0 + width - 1);
+            const int xlo = mx > 1 ? px0 - 1 : 0;
+            const int xhi = mx > 1 ? min(px1 + 1, xlo + mx - 1) : 0;
+            unsigned long long total = 0;
+            for (int row = 0; row < ny * nz; row++) {
+                const int dy_row = ny > 1 ? (row % ny) - 1 : 0, dz_row = nz > 1 ? (row / ny) - 1 : 0;
+                const int yy = wrap_index(yc + dy_row, my), zz = wrap_index(zc + dz_row, mz);
+                const uint32_t base = world_base + (uint32_t)((zz * my + yy) * mx);
+                for (int half = 0; half < 2; half++) {
+                    int a = xlo, b = xhi;
+                    if (xlo < 0) {
+                        if (half == 0) a = 0;
+                        else { a = xlo + mx; b = mx - 1; }
+                    } else if (xhi >= mx) {
+                        if (half == 0) b = mx - 1;
+                        else { a = 0; b = xhi - mx; }
+                    } else if (half == 1) {
+                        b = a - 1;
+                    }
+                    if (b >= a) total += cell_off[base + b + 1] - cell_off[base + a];
+                }
+            }
+            // the homes of this pass: those whose cell lies in [px0, px1]
+            int homes = 0;
+            for (int q = 0; q < it.count; q++) {
+                const int hx = (int)(keys_sorted[it.first + q] - row_base);
+                homes += (generic || (hx >= px0 && hx <= px1)) ? 1 : 0;
+            }
+            staged += total;
+            tested += total * (unsigned long long)homes;
+        }
+    }
+    // one atomic per warp
+    for (int o = 16; o > 0; o >>= 1) {
+        staged += __shfl_down_sync(0xffffffffu, staged, o);
+        tested += __shfl_down_sync(0xffffffffu, tested, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (staged | tested)) {
+        atomicAdd(&out[0], staged);
+        atomicAdd(&out[1], tested);
+    }
 }
 
 // Items: each row of cells (rows = (y, z) pairs) cut into chunks of at most
@@ -987,6 +1181,17 @@ cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const 
 }
 
 }  // namespace
+
+cudaError_t launch_force_work(const StepConsts& c, const uint32_t* keys_sorted, const uint32_t* cell_off,
+                              const Item* items, const int* n_items, int max_items, unsigned long long* out,
+                              cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess || max_items <= 0) return e;
+    force_work_kernel<<<(max_items + 255) / 256, 256, 0, st>>>(c, keys_sorted, cell_off, items, n_items, out);
+    note_launches(st);
+    return cudaGetLastError();
+}
 
 int max_step_items(int n, const Grid& g) { return (n + 31) / 32 + g.worlds * g.m[1] * g.m[2]; }
 

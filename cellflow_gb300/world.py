@@ -258,6 +258,13 @@ class ParticleSimulation:
                                            _ptr(end), cells), "cf_debug_cell_list")
         return g, cell_of, order, start, end
 
+    def force_work(self, params: SimulationParams) -> tuple[int, int]:
+        """(candidates staged, candidate tests) of the force kernel's filter for the current state."""
+        p = params.to_c()
+        staged, tested = C.c_uint64(), C.c_uint64()
+        check(self._lib.cf_force_work(self._h, C.byref(p), C.byref(staged), C.byref(tested)), "cf_force_work")
+        return staged.value, tested.value
+
     def work_counters(self, params: SimulationParams) -> tuple[int, int]:
         c27 = C.c_uint64()
         inter = C.c_uint64()

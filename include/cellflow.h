@@ -270,6 +270,13 @@ int cf_debug_cell_list(cf_world* w, const cf_step_params* p, uint32_t* cell_of, 
  * work model (cells per axis floor(L/r_max)): directed candidate pairs in
  * the 27-cell stencil (C27) and directed interacting pairs (I). */
 int cf_work_counters(cf_world* w, const cf_step_params* p, uint64_t* c27, uint64_t* interacting);
+/* The force kernel's filter work for the current state (no counterpart in the
+ * reference): the candidates its items stage (the union of each item's homes'
+ * 27-cell stencils, summed over items) and the candidate tests of the items'
+ * particles (staged x particles per item).  tested / n against the work model's
+ * C27 / n is the filter's excess over the canonical stencil.  Builds the step's
+ * cell list; the particle state is unchanged. */
+int cf_force_work(cf_world* w, const cf_step_params* p, uint64_t* staged, uint64_t* tested);
 
 /* ---- proximity graph ---------------------------------------------------- */
 

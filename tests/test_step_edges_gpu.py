@@ -173,3 +173,25 @@ def test_skewed_occupancy_under_lane_pairing(cflib, variant):
                                  label=f"blobs, variant {variant}")
     med = np.median(counts)
     assert counts.max() > 2 * med and counts.min() < med / 4
+
+
+@pytest.mark.parametrize("variant", [1, 2, 12])
+def test_lattice_at_the_threshold_overflows_the_band_list(cflib, variant):
+    """A cubic lattice whose spacing puts every nearest-neighbour pair within rounding of
+    the interaction threshold: each of an item's homes has six such band pairs, far more
+    per batch than the drain lists (64), so the batch's band pairs are found again by
+    re-walking every home's hits; the neighbour counts stay bit-exact against the oracle,
+    pairs across the periodic boundary included."""
+    m, T, r = 10, 3, 0.1
+    a = np.float32(np.sqrt(np.float32(r) * np.float32(r) - np.float32(1e-4)))
+    W = float(np.float32(m) * a)
+    k = np.arange(m, dtype=np.float32)
+    g = np.stack(np.meshgrid(k, k, k, indexing="ij"), axis=-1).reshape(-1, 3)
+    pos = ((g + np.float32(0.5)) * a).astype(np.float32)
+    # a jitter of a few ulp of the spacing puts the pairs on both sides of the threshold
+    pos = (pos + np.random.default_rng(8).uniform(-3e-7, 3e-7, pos.shape)).astype(np.float32)
+    types = (np.arange(len(pos)) % T).astype(np.uint32)
+    table = np.random.default_rng(9).normal(0, 0.5, (T, T)).astype(np.float32)
+    params = params_for(T, r, W, W, W)
+    rec, counts = step_vs_oracle(pos, types, table, params, variant=variant, label=f"lattice, variant {variant}")
+    assert 0 < counts.mean() < 6.0

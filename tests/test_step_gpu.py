@@ -318,6 +318,24 @@ def test_work_counters(cflib):
     assert c27 == int(round(oracle.c27(rec["pos"], m, inv)))
 
 
+def test_force_work_bounds(cflib):
+    """cf_force_work: every particle is staged by its own item, every interacting pair is
+    among the candidates tested, and no item tests more than 32 particles' worth."""
+    w = inputs.Workload("fw", n=20000, num_types=4, radius=0.1, steps=1, seed=23)
+    sim, pos, types, table, radio = make_world(w)
+    params = w.params()
+    staged, tested = sim.force_work(params)
+    before = sim.get_state()
+    sim.simulate(params, 1)
+    counts = sim.getNeighborCounts()
+    c27, _ = sim.work_counters(params)
+    sim.close()
+    assert staged >= w.n and int(counts.sum()) <= tested <= 32 * staged
+    assert tested >= int(counts.sum()) + w.n  # every particle also tests itself (masked out)
+    print(f"\nfilter tests per particle {tested / w.n:.1f}, staged per particle {staged / w.n:.2f}")
+    assert before[0].shape[0] == w.n
+
+
 @pytest.mark.parametrize("wl", ["plain_n100k_t8", "blobs_n1m_t12"])
 def test_full_size_sampled_rows(cflib, wl):
     """Full-size configurations: a strided sample of particles against the oracle, which
