@@ -127,9 +127,7 @@ struct PairScratch {
     uint32_t nzw[32];
     uint32_t pairing[32];
 };
-struct NoScratch {
-    float4 home_h[32];
-};
+struct NoScratch {};
 // Balanced drain: each lane's home and filter operands, group bitmap and hit
 // count for the batch, and the partial sums of the (lane, home) pieces of the
 // task line, at index lane + rank of the home among the homes with hits.
@@ -142,13 +140,6 @@ struct BalScratch {
 };
 
 // Per-warp staging area, kStage candidates (a multiple of 32) per batch.
-// Band pairs of a batch: filter hits whose staged distance is within rounding
-// of the threshold.  The drain lists them (a rarely taken, warp-uniform branch)
-// and they are resolved after it with the reference's exact test, so the
-// drain's trips carry no exact-test code; a batch with more than kBandCap of
-// them re-walks its homes' hits instead.
-constexpr int kBandCap = 64;
-
 // Drain modes: 0 one lane per home, 1 lanes paired (busiest with idlest),
 // 2 balanced (the batch's hits split evenly over the lanes).
 template <int kMode>
@@ -162,8 +153,6 @@ struct WarpSmem {
     uint32_t meta[kStage];              // sorted index | type << 27
     uint32_t mask[(kStage / 32) * 32];  // [group][lane]
     float origin[4];                    // the pass's staging origin (x, y, z)
-    uint32_t band[kBandCap];            // band pairs of the batch: slot | home lane << 16
-    float4 band_acc[32];                // per home: force and count of its band pairs, all batches
     DrainScratch<kMode> pr;
 };
 
@@ -230,26 +219,16 @@ __device__ __forceinline__ void staged_delta(const StepConsts& c, float cx, floa
 // fallback.  Returns the staged displacement and its contracted d^2.
 // `origin` is the pass's staging origin (unused on generic grids).
 template <bool kGeneric, bool kUniformR>
-__device__ __forceinline__ bool pair_certain(const StepConsts& c, const Lane& L, const HomeOps& H, float cx, float cy,
-                                             float cz, uint32_t meta, const Tables& tb, float& dx, float& dy,
-                                             float& dz, float& d2)
-{
-    staged_delta<kGeneric>(c, cx, cy, cz, L.h, H, dx, dy, dz);
-    d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    const uint32_t pair = L.tp * kTableStride + (meta >> kTypeShift);
-    return d2 < (kUniformR ? c.thr_lo_uniform : tb.thr_lo[pair]);
-}
-
-// The full test: the certain-interaction bound, then the reference's exact test
-// for a pair within rounding of the threshold.
-template <bool kGeneric, bool kUniformR>
 __device__ __forceinline__ bool pair_test(const StepConsts& c, const Lane& L, const HomeOps& H,
                                           const float* origin, float cx, float cy, float cz, uint32_t meta,
                                           const float4* __restrict__ pos_sorted, const Tables& tb, float& dx,
                                           float& dy, float& dz, float& d2)
 {
-    const uint32_t pair = L.tp * kTableStride + (meta >> kTypeShift);
-    bool inter = pair_certain<kGeneric, kUniformR>(c, L, H, cx, cy, cz, meta, tb, dx, dy, dz, d2);
+    staged_delta<kGeneric>(c, cx, cy, cz, L.h, H, dx, dy, dz);
+    d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const uint32_t other = meta >> kTypeShift;
+    const uint32_t pair = L.tp * kTableStride + other;
+    bool inter = d2 < (kUniformR ? c.thr_lo_uniform : tb.thr_lo[pair]);
     if (!inter) {
         // within rounding of the threshold: the reference's exact test
         const float4 o = pos_sorted[meta & kIndexMask];
@@ -360,8 +339,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     L.tp = __float_as_uint(L.h.w) & kTypeMask;
     L.fx = L.fy = L.fz = 0.0f;
     L.count = 0;
-    w.pr.home_h[lane] = L.h;
-    w.band_acc[lane] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 
     // cell coordinates inside the item's world (items never straddle worlds or rows)
     const int mx = c.grid.m[0], my = c.grid.m[1], mz = c.grid.m[2];
@@ -426,7 +403,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 w.origin[1] = oy;
                 w.origin[2] = oz;
             }
-            if constexpr (kBalance || kBal) w.pr.home_m2[lane] = make_float4(H.m2x.x, H.m2y.x, H.m2z.x, 0.0f);
+            if constexpr (kBalance || kBal) {
+                w.pr.home_h[lane] = L.h;
+                w.pr.home_m2[lane] = make_float4(H.m2x.x, H.m2y.x, H.m2z.x, 0.0f);
+            }
         } else {
             H.m2x = H.m2y = H.m2z = H.k = make_float2(0.0f, 0.0f);
         }
@@ -588,22 +568,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             // the top part of its partner's hits with its partner's home, accumulating them
             // apart; the partner adds that partial after the trips.  Each pair's work is then
             // about half its total.
-            const uint32_t nz_own = nz;  // this lane's own groups with hits (the overflow re-walk)
-            int nband = 0;               // band pairs listed in this batch (warp-uniform)
-            bool band_overflow = false;
-            // list the band pairs of one trip (bit q of `band`: pair q of this lane)
-            auto list_band = [&](uint32_t band, const int* slot, int home) {
-                if (!__any_sync(0xffffffffu, band != 0u)) return;
-#pragma unroll
-                for (int q = 0; q < kPer; q++) {
-                    const bool mine = (band >> q) & 1u;
-                    const uint32_t b = __ballot_sync(0xffffffffu, mine);
-                    if (nband + __popc(b) > kBandCap) band_overflow = true;
-                    if (!band_overflow && mine)
-                        w.band[nband + __popc(b & ((1u << lane) - 1u))] = (uint32_t)slot[q] | ((uint32_t)home << 16);
-                    if (!band_overflow) nband += __popc(b);
-                }
-            };
             if constexpr (kBal) {
                 // ---- balanced drain: the batch's H hits, home by home in lane order, form a
                 // task line; lane l takes tasks [l H / 32, (l + 1) H / 32), walking each home's
@@ -685,7 +649,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     const int nq = min(kPer, inh);
                     int slot[kPer];
                     bool valid[kPer];
-                    uint32_t band = 0u;
 #pragma unroll
                     for (int q = 0; q < kPer; q++) {
                         valid[q] = q < nq;
@@ -705,10 +668,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         float x, y, z;
                         staged_xyz(xyf, zcf, slot[q], x, y, z);
                         meta[q] = w.meta[slot[q]];
-                        const bool certain = pair_certain<kGeneric, kUniformR>(c, L, H, x, y, z, meta[q], tb, dx[q],
-                                                                               dy[q], dz[q], d2[q]);
-                        inter[q] = valid[q] && certain;
-                        band |= (valid[q] && !certain ? 1u : 0u) << q;
+                        inter[q] = valid[q] && pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta[q],
+                                                                              pos_sorted, tb, dx[q], dy[q], dz[q],
+                                                                              d2[q]);
                     }
 #pragma unroll
                     for (int q = 0; q < kPer; q++) wgt[q] = pair_weight<kUniformR>(d2[q], meta[q], L, tb, c1u);
@@ -723,7 +685,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     }
                     inh -= nq;
                     left -= nq;
-                    list_band(band, slot, hm);
                 }
                 if (worked)
                     w.pr.part[lane + __popc(has & ((1u << hm) - 1u))] =
@@ -832,9 +793,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         upto = kPer * it + fw;
                     }
                 }
-                int slot[kPer];
-                uint32_t band = 0u;
                 if (kPer * it < upto) {
+                    int slot[kPer];
                     bool valid[kPer];
 #pragma unroll
                     for (int q = 0; q < kPer; q++) {
@@ -855,10 +815,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         float x, y, z;
                         staged_xyz(xyf, zcf, slot[q], x, y, z);
                         meta[q] = w.meta[slot[q]];
-                        const bool certain = pair_certain<kGeneric, kUniformR>(c, L, H, x, y, z, meta[q], tb, dx[q],
-                                                                               dy[q], dz[q], d2[q]);
-                        inter[q] = certain && valid[q];
-                        band |= (!certain && valid[q] ? 1u : 0u) << q;
+                        inter[q] = pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta[q], pos_sorted, tb,
+                                                                  dx[q], dy[q], dz[q], d2[q]) &&
+                                   valid[q];
                     }
 #pragma unroll
                     for (int q = 0; q < kPer; q++) wgt[q] = pair_weight<kUniformR>(d2[q], meta[q], L, tb, c1u);
@@ -872,7 +831,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         }
                     }
                 }
-                list_band(band, slot, src);
             }
             if constexpr (kBalance) {
                 // a light lane that switched holds its partner's partial: hand it over and
@@ -902,92 +860,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 }
             }
             }
-            // ---- band pairs, every lane back on its own home: listed ones resolved in
-            // parallel (lane e takes entry e) and added by their homes in list order; after
-            // an overflow, every lane re-walks its own hits of the batch for them instead.
-            // They go to the home's band accumulator, in the order the homes' hits are
-            // concatenated whatever the batch size, and join its sums once, after the last
-            // batch
-            __syncwarp();
-            if (band_overflow) {
-                uint32_t zz = nz_own;
-                while (zz) {
-                    const int g = __ffs(zz) - 1;
-                    zz &= zz - 1u;
-                    uint32_t mm = w.mask[g * 32 + lane];
-                    while (mm) {
-                        const int slot = g * 32 + (__ffs(mm) - 1);
-                        mm &= mm - 1u;
-                        float x, y, z, dx, dy, dz, d2;
-                        staged_xyz(xyf, zcf, slot, x, y, z);
-                        const uint32_t meta = w.meta[slot];
-                        if (pair_certain<kGeneric, kUniformR>(c, L, H, x, y, z, meta, tb, dx, dy, dz, d2)) continue;
-                        if (pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta, pos_sorted, tb, dx, dy,
-                                                           dz, d2)) {
-                            const float wgt = pair_weight<kUniformR>(d2, meta, L, tb, c1u);
-                            float4 a = w.band_acc[lane];
-                            a.x = fmaf(dx, wgt, a.x);
-                            a.y = fmaf(dy, wgt, a.y);
-                            a.z = fmaf(dz, wgt, a.z);
-                            a.w += 1.0f;
-                            w.band_acc[lane] = a;
-                        }
-                    }
-                }
-            } else {
-                for (int e0 = 0; e0 < nband; e0 += 32) {
-                    float bx = 0.0f, by = 0.0f, bz = 0.0f;
-                    int bc = 0, bhome = -1;
-                    if (e0 + lane < nband) {
-                        const uint32_t ent = w.band[e0 + lane];
-                        const int slot = (int)(ent & 0xffffu);
-                        bhome = (int)(ent >> 16);
-                        Lane Lb;
-                        Lb.h = w.pr.home_h[bhome];
-                        Lb.tp = __float_as_uint(Lb.h.w) & kTypeMask;
-                        HomeOps Hb;
-                        Hb.m2x = make_float2(-2.0f * (Lb.h.x - w.origin[0]), 0.0f);
-                        Hb.m2y = make_float2(-2.0f * (Lb.h.y - w.origin[1]), 0.0f);
-                        Hb.m2z = make_float2(-2.0f * (Lb.h.z - w.origin[2]), 0.0f);
-                        float x, y, z, dx, dy, dz, d2;
-                        staged_xyz(xyf, zcf, slot, x, y, z);
-                        const uint32_t meta = w.meta[slot];
-                        if (pair_test<kGeneric, kUniformR>(c, Lb, Hb, w.origin, x, y, z, meta, pos_sorted, tb, dx, dy,
-                                                           dz, d2)) {
-                            const float wgt = pair_weight<kUniformR>(d2, meta, Lb, tb, c1u);
-                            bx = dx * wgt;
-                            by = dy * wgt;
-                            bz = dz * wgt;
-                            bc = 1;
-                        }
-                    }
-                    const int cnt = min(32, nband - e0);
-                    for (int e = 0; e < cnt; e++) {
-                        const int hme = __shfl_sync(0xffffffffu, bhome, e);
-                        const float ex = __shfl_sync(0xffffffffu, bx, e), ey = __shfl_sync(0xffffffffu, by, e),
-                                    ez = __shfl_sync(0xffffffffu, bz, e);
-                        const int ec = __shfl_sync(0xffffffffu, bc, e);
-                        if (lane == hme) {
-                            float4 a = w.band_acc[lane];
-                            a.x += ex;
-                            a.y += ey;
-                            a.z += ez;
-                            a.w += (float)ec;
-                            w.band_acc[lane] = a;
-                        }
-                    }
-                }
-            }
             __syncwarp();
         }
-    }
-    {
-        __syncwarp();
-        const float4 a = w.band_acc[lane];
-        L.fx += a.x;
-        L.fy += a.y;
-        L.fz += a.z;
-        L.count += (int)a.w;
     }
     if (split > 1) {
         // the item's warps meet at a named barrier (id 1 + item slot, 32 * split threads);
