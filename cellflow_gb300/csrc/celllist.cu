@@ -418,17 +418,67 @@ __global__ void __launch_bounds__(kThreads)
     if (i < n) unsorted[cell_off[keys[i]] + slot[i]] = (uint32_t)i;
 }
 
+// Cells of more than this many particles are ranked by the warp-wide method
+// below when a warp's 32 positions all lie in one of them.
+constexpr uint32_t kRankWarpMin = 64;
+
 __global__ void __launch_bounds__(kThreads)
     rank_gather_kernel(const uint32_t* __restrict__ unsorted, const uint32_t* __restrict__ keys,
                        const uint32_t* __restrict__ cell_off, const float4* __restrict__ pos, int n,
                        uint32_t* __restrict__ vals_sorted, uint32_t* __restrict__ keys_sorted,
                        float4* __restrict__ pos_sorted)
 {
+    __shared__ uint32_t s_hist[kWarps][33];
     const int p = blockIdx.x * kThreads + threadIdx.x;
-    if (p >= n) return;
-    const uint32_t i = unsorted[p];
-    const uint32_t key = keys[i];
-    const uint32_t b = cell_off[key], e = cell_off[key + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool valid = p < n;
+    uint32_t i = valid ? unsorted[p] : 0u;
+    const uint32_t key = valid ? keys[i] : 0xffffffffu;
+    const uint32_t b = valid ? cell_off[key] : 0u, e = valid ? cell_off[key + 1] : 0u;
+    const uint32_t key0 = __shfl_sync(0xffffffffu, key, 0);
+    if (__all_sync(0xffffffffu, valid && key == key0) && e - b > kRankWarpMin) {
+        // The warp's 32 positions lie in one large cell [b, e).  Sort the warp's own
+        // particle indices (bitonic over shuffles: lane j then holds the j-th smallest,
+        // s_j).  For every entry x of the cell, c(x) = #{j : s_j <= x} by a binary
+        // search over the lanes; x < s_j exactly when c(x) <= j, so the rank of s_j in
+        // the cell is the number of entries with c(x) <= j: a histogram of c, summed.
+        uint32_t v = i;
+#pragma unroll
+        for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                const uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+                v = (((lane & j) == 0) == ((lane & k) == 0)) ? min(v, o) : max(v, o);
+            }
+        }
+        s_hist[warp][lane] = 0u;
+        if (lane == 0) s_hist[warp][32] = 0u;
+        __syncwarp();
+        for (uint32_t q0 = b; q0 < e; q0 += 32u) {
+            const uint32_t q = q0 + (uint32_t)lane;
+            const uint32_t x = q < e ? unsorted[q] : 0u;
+            int c = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1)
+                if (__shfl_sync(0xffffffffu, v, c + step - 1) <= x) c += step;
+            if (__shfl_sync(0xffffffffu, v, c) <= x && c == 31) c = 32;  // x >= s_31
+            if (q < e) atomicAdd(&s_hist[warp][c], 1u);
+        }
+        __syncwarp();
+        uint32_t rank = s_hist[warp][lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, rank, o);
+            if (lane >= o) rank += y;
+        }
+        i = v;
+        const uint32_t dst = b + rank;
+        vals_sorted[dst] = i;
+        keys_sorted[dst] = key;
+        pos_sorted[dst] = pos[i];
+        return;
+    }
+    if (!valid) return;
     uint32_t rank = 0;
     for (uint32_t q = b; q < e; q++) rank += unsorted[q] < i ? 1u : 0u;
     const uint32_t dst = b + rank;
