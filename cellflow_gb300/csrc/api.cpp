@@ -216,7 +216,6 @@ void free_particles(cf_world* w)
     dev_free(s.mesh_slots);
     dev_free(s.mesh_count);
     dev_free(s.out_idx);
-    dev_free(s.colors);
     dev_free(s.counters);
     dev_free(s.cell_pop);
     dev_free(s.row_count);
@@ -362,18 +361,16 @@ int ensure_out(cf_world* w, size_t entries)
 
 // The colours of a vertex call, one per type, into the world's fixed colour
 // array (ordered on the stream before the kernel that reads them).
-int upload_colors(cf_world* w, const cf_color* colors)
+// The per-type colours as the emit kernels' by-value table.
+ColorTable color_table(const cf_world* w, const cf_color* colors)
 {
-    Scratch& s = w->s;
-    if (!s.colors) CF_CUDA(dev_alloc(&s.colors, 3 * (size_t)CF_MAX_TYPES));
-    float tmp[3 * CF_MAX_TYPES];
-    for (int t = 0; t < w->num_types; t++) {
-        tmp[3 * t] = colors[t].r;
-        tmp[3 * t + 1] = colors[t].g;
-        tmp[3 * t + 2] = colors[t].b;
+    ColorTable t{};
+    for (int k = 0; k < w->num_types; k++) {
+        t.c[3 * k] = colors[k].r;
+        t.c[3 * k + 1] = colors[k].g;
+        t.c[3 * k + 2] = colors[k].b;
     }
-    CF_CUDA(cudaMemcpyAsync(s.colors, tmp, sizeof(float) * 3 * w->num_types, cudaMemcpyHostToDevice, w->stream));
-    return CF_OK;
+    return t;
 }
 
 // Wait for the world's stream and turn the device error word into a status.
@@ -1754,10 +1751,12 @@ int proximity_enqueue(cf_world* w, float distance, int max_conn)
     Scratch& s = w->s;
     const float dsq = distance * distance;  // ParticleSimulation.cu:660
     return run_selection(w, 0, g, dsq, max_conn, [&]() -> int {
-        // the step's tiled cell list on the proximity grid: cell c holds cell_off[c] .. cell_off[c + 1]
+        // the tiled cell list on the proximity grid, unordered within a cell (the selection
+        // keeps the smallest qualifying indices whatever the order): cell c holds
+        // cell_off[c] .. cell_off[c + 1]
         int which = 0;
         CF_CUDA(launch_cell_list_csr(w->pos, w->n, g, w->ext, w->num_types, s, s.cell_off, nullptr, nullptr, w->err,
-                                     &which, w->stream));
+                                     &which, w->stream, false));
         CF_CUDA(cudaMemsetAsync(s.prox_count + w->n, 0, sizeof(uint32_t), w->stream));
         CF_CUDA(launch_proximity_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.cell_off + 1, true, g,
                                         w->n, dsq, max_conn, s.prox_slots, s.prox_count, w->stream));
@@ -1789,7 +1788,7 @@ int mesh_enqueue(cf_world* w, float distance, int max_conn)
     return run_selection(w, 1, g, dsq, max_conn, [&]() -> int {
         int which = 0;
         CF_CUDA(launch_cell_list_csr(w->pos, w->n, g, w->ext, w->num_types, s, s.cell_off, nullptr, nullptr, w->err,
-                                     &which, w->stream));
+                                     &which, w->stream, false));
         CF_CUDA(cudaMemsetAsync(s.mesh_count + w->n, 0, sizeof(uint32_t), w->stream));
         CF_CUDA(launch_mesh_select(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, s.cell_off + 1, g, w->n,
                                    dsq, std::min(max_conn, CF_MESH_MAX_CONN), s.mesh_slots, s.mesh_count, w->stream));
@@ -1826,7 +1825,7 @@ int cf_triangle_mesh(cf_world* w, float distance, int max_conn, int32_t* triangl
     if (write > 0) {
         rc = ensure_out(w, 3 * (size_t)write);
         if (rc) return rc;
-        CF_CUDA(launch_mesh_emit(w->s.mesh_slots, w->s.mesh_count, w->n, w->pos, nullptr, 1, w->s.out_idx, nullptr,
+        CF_CUDA(launch_mesh_emit(w->s.mesh_slots, w->s.mesh_count, w->n, w->pos, ColorTable{}, 1, w->s.out_idx, nullptr,
                                  write, w->stream));
         rc = copy_out(w, triangles, 3 * (size_t)write);
         if (rc) return rc;
@@ -1849,10 +1848,8 @@ int cf_triangle_mesh_device(cf_world* w, float distance, int max_conn, const cf_
     if (rc) return rc;
     if (cap_vertices >= 3) {
         // ParticleSimulation.cu:356 indexes colours by type % numParticleTypes
-        rc = upload_colors(w, colors);
-        if (rc) return rc;
-        CF_CUDA(launch_mesh_emit(w->s.mesh_slots, w->s.mesh_count, w->n, w->pos, w->s.colors, w->num_types, nullptr,
-                                 vertices, cap_vertices / 3, w->stream));
+        CF_CUDA(launch_mesh_emit(w->s.mesh_slots, w->s.mesh_count, w->n, w->pos, color_table(w, colors),
+                                 w->num_types, nullptr, vertices, cap_vertices / 3, w->stream));
     }
     rc = sync_and_check(w);
     if (rc) return rc;
@@ -1898,10 +1895,9 @@ int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, cons
     if (rc) return rc;
     if (cap_vertices > 0) {
         // ParticleSimulation.cu:253 indexes colours by type % numParticleTypes
-        rc = upload_colors(w, colors);
-        if (rc) return rc;
-        CF_CUDA(launch_proximity_emit_vertices(w->s.prox_slots, w->s.prox_count, w->n, max_conn, w->pos, w->s.colors,
-                                               w->num_types, vertices, cap_vertices, w->stream));
+        CF_CUDA(launch_proximity_emit_vertices(w->s.prox_slots, w->s.prox_count, w->n, max_conn, w->pos,
+                                               color_table(w, colors), w->num_types, vertices, cap_vertices,
+                                               w->stream));
     }
     rc = sync_and_check(w);
     if (rc) return rc;

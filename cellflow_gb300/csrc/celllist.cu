@@ -418,6 +418,24 @@ __global__ void __launch_bounds__(kThreads)
     if (i < n) unsorted[cell_off[keys[i]] + slot[i]] = (uint32_t)i;
 }
 
+// Unordered cell list: particle i straight to offset[cell] + arrival slot,
+// with its value, key and position (callers that do not depend on the order
+// within a cell).
+__global__ void __launch_bounds__(kThreads)
+    place_gather_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ slot,
+                        const uint32_t* __restrict__ cell_off, const float4* __restrict__ pos, int n,
+                        uint32_t* __restrict__ vals_sorted, uint32_t* __restrict__ keys_sorted,
+                        float4* __restrict__ pos_sorted)
+{
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t key = keys[i];
+    const uint32_t dst = cell_off[key] + slot[i];
+    vals_sorted[dst] = (uint32_t)i;
+    keys_sorted[dst] = key;
+    pos_sorted[dst] = pos[i];
+}
+
 // Cells of more than this many particles are ranked by the warp-wide method
 // below when a warp's 32 positions all lie in one of them.
 constexpr uint32_t kRankWarpMin = 64;
@@ -694,7 +712,7 @@ int cell_list_tiles(const Grid& g)
 
 cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
                                  Scratch& s, uint32_t* cell_off, Item* items, int* n_items, int* err, int* which,
-                                 cudaStream_t st)
+                                 cudaStream_t st, bool stable)
 {
     cudaError_t e = cudaMemsetAsync(cell_off, 0, sizeof(uint32_t) * ((size_t)g.cells + 1), st);
     if (e != cudaSuccess) return e;
@@ -727,7 +745,11 @@ cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const 
     tile_apply_kernel<<<tiles, kTileThreads, 0, st>>>(cell_off, tg, s.tile_sums, items, n_items);
     note_launches(st);
     *which = 1;
-    if (n > 0) {
+    if (n > 0 && !stable) {
+        place_gather_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.keys[0], s.aux, cell_off, pos, n,
+                                                                          s.vals[1], s.keys[1], s.pos_sorted);
+        note_launches(st);
+    } else if (n > 0) {
         place_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.keys[0], s.aux, cell_off, n, s.vals[0]);
         note_launches(st);
         rank_gather_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.vals[0], s.keys[0], cell_off, pos, n,

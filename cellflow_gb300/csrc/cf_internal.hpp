@@ -109,7 +109,6 @@ struct Scratch {
     // device staging of index output bound for host memory (edges, triangles)
     int32_t* out_idx = nullptr;
     size_t out_cap = 0;  // int32 entries
-    float* colors = nullptr;  // CF_MAX_TYPES * 3 floats: the colours of the last vertex call
     // work counters
     unsigned long long* counters = nullptr;  // [0] C27, [1] I
     uint32_t* cell_pop = nullptr;            // canonical-grid populations
@@ -332,10 +331,13 @@ int cell_list_launches(int n, int key_bits);
 // (s.keys[*which], s.vals[*which], stable: cell order, ties in index order),
 // the position snapshot s.pos_sorted and, when items is not null, the force
 // kernel's row-aligned items.  Rows of at most kTileCellsMax cells take the
-// tiled path (5 kernels); longer rows a radix sort.
+// tiled path (5 kernels); longer rows a radix sort.  stable = false (for
+// callers whose result does not depend on the order within a cell) leaves the
+// particles of a cell in arrival order and saves the stable ranking on the
+// tiled path (4 kernels).
 cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const float* ext, int num_types,
                                  Scratch& s, uint32_t* cell_off, Item* items, int* n_items, int* err, int* which,
-                                 cudaStream_t st);
+                                 cudaStream_t st, bool stable = true);
 int cell_list_csr_buffer(int n, const Grid& g);
 int cell_list_csr_launches(int n, const Grid& g, bool with_plan);
 int cell_list_tiles(const Grid& g);  // 0 when the rows are longer than a tile
@@ -349,14 +351,18 @@ cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* ke
 cudaError_t launch_mesh_select(const float4* pos_sorted, const uint32_t* keys_sorted, const uint32_t* vals_sorted,
                                const uint32_t* cell_start, const uint32_t* cell_end, const Grid& g, int n, float dsq,
                                int max_conn, int32_t* slots, uint32_t* count, cudaStream_t st);
+// Per-type colours (r, g, b), passed to the emit kernels by value.
+struct ColorTable {
+    float c[3 * CF_MAX_TYPES];
+};
 cudaError_t launch_mesh_emit(const int32_t* slots, const uint32_t* offsets, int n, const float4* pos,
-                             const float* colors, int n_colors, int32_t* tris, float* vertices, long long cap_tris,
+                             const ColorTable& colors, int n_colors, int32_t* tris, float* vertices, long long cap_tris,
                              cudaStream_t st);
 cudaError_t launch_proximity_emit_edges(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,
                                         int32_t* edges, int cap, cudaStream_t st);
 cudaError_t launch_proximity_emit_vertices(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,
-                                           const float4* pos, const float* colors, int n_colors, float* vertices,
-                                           int cap_vertices, cudaStream_t st);
+                                           const float4* pos, const ColorTable& colors, int n_colors,
+                                           float* vertices, int cap_vertices, cudaStream_t st);
 cudaError_t launch_init_particles(float4* pos, float4* vel, float4* acc, int* counts, int n, int num_types,
                                   const float* lo, const float* span, uint64_t seed, cudaStream_t st,
                                   uint32_t world = 0);

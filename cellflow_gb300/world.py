@@ -282,10 +282,18 @@ class ParticleSimulation:
               "cf_triangle_mesh")
         return tris[: count.value].copy()
 
+    def _color_array(self, colors):
+        """The colours as a ctypes array, rebuilt only when they change between calls."""
+        key = [tuple(c) for c in colors]
+        if getattr(self, "_colors_key", None) != key:
+            self._colors_key = key
+            self._colors_arr = (Color * len(key))(*[Color(*c) for c in key])
+        return self._colors_arr
+
     def triangle_mesh_device(self, distance: float, max_conn: int, colors, vertices_ptr: int,
                              cap_vertices: int) -> int:
         """The reference's 9-float triangle vertices into a device buffer; returns the vertex count."""
-        cols = (Color * len(colors))(*[Color(*c) for c in colors])
+        cols = self._color_array(colors)
         count = C.c_int()
         check(self._lib.cf_triangle_mesh_device(self._h, distance, max_conn, cols, len(colors),
                                                 C.c_void_p(vertices_ptr), cap_vertices, C.byref(count)),
@@ -365,7 +373,7 @@ class ParticleSimulation:
 
     def proximity_vertices_device(self, distance: float, max_conn: int, colors, vertices_ptr: int,
                                   cap_vertices: int) -> int:
-        cols = (Color * len(colors))(*[Color(*c) for c in colors])
+        cols = self._color_array(colors)
         count = C.c_int()
         check(self._lib.cf_proximity_vertices_device(self._h, distance, max_conn, cols, len(colors),
                                                      C.c_void_p(vertices_ptr), cap_vertices, C.byref(count)),
