@@ -1,16 +1,19 @@
 """ctypes binding of the C ABI in include/cellflow.h.
 
-The library is the in-tree ``libcellflow.so`` built for sm_103a.  Loading
-fails loudly when it is missing: there is no CPU fallback for the step.
+The library is the in-tree ``libcellflow.so`` built for sm_103a
+(``libcellflow_bounds.so``, the bounds-checked build, when the environment
+sets CELLFLOW_LIBRARY=bounds).  Loading fails loudly when it is missing:
+there is no CPU fallback for the step.
 """
 
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 _PKG = Path(__file__).resolve().parent
-LIB_PATH = _PKG / "libcellflow.so"
+LIB_PATH = _PKG / ("libcellflow_bounds.so" if os.environ.get("CELLFLOW_LIBRARY") == "bounds" else "libcellflow.so")
 
 CF_OK = 0
 CF_ERR_INVALID = -1
@@ -191,6 +194,9 @@ _SIGNATURES = {
     ),
     "cf_work_counters": (C.c_int, [_W, _P(StepParams), _P(C.c_uint64), _P(C.c_uint64)]),
     "cf_force_work": (C.c_int, [_W, _P(StepParams), _P(C.c_uint64), _P(C.c_uint64)]),
+    "cf_debug_bounds": (C.c_int, [_P(C.c_int), _P(C.c_int), C.c_char_p, C.c_int, _P(C.c_longlong),
+                                  _P(C.c_longlong)]),
+    "cf_debug_force_bad_item": (C.c_int, [_W, _P(StepParams), C.c_int]),
     "cf_proximity_edges": (C.c_int, [_W, C.c_float, C.c_int, C.c_void_p, C.c_int, _P(C.c_int)]),
     "cf_proximity_vertices_device": (
         C.c_int,

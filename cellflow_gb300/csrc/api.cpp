@@ -79,7 +79,13 @@ cudaError_t raw_alloc(void** p, size_t bytes)
     }
     const cudaError_t inj = injected_error("cudaMalloc");
     if (inj != cudaSuccess) return inj;
+#ifdef CF_DEBUG_BOUNDS
+    // the bounds-checked build pads every buffer, so an index that a check missed
+    // a little past the end still lands in this allocation
+    const cudaError_t e = cudaMalloc(p, bytes + (64u << 10));
+#else
     const cudaError_t e = cudaMalloc(p, bytes);
+#endif
     if (e != cudaSuccess) {
         *p = nullptr;
         return e;
@@ -1662,6 +1668,62 @@ int cf_force_work(cf_world* w, const cf_step_params* p, uint64_t* staged, uint64
     if (staged) *staged = host[0];
     if (tested) *tested = host[1];
     return CF_OK;
+}
+
+int cf_debug_bounds(int* checked, int* found, char* where, int where_cap, long long* index, long long* limit)
+{
+#ifdef CF_DEBUG_BOUNDS
+    if (checked) *checked = 1;
+#else
+    if (checked) *checked = 0;
+#endif
+    if (found) *found = 0;
+    if (where && where_cap > 0) where[0] = 0;
+    const struct {
+        const char* file;
+        cudaError_t (*take)(BoundsRecord*);
+    } units[] = {{"celllist.cu", bounds_take_celllist}, {"step.cu", bounds_take_step},
+                 {"proximity.cu", bounds_take_proximity}};
+    bool first = true;
+    for (const auto& u : units) {
+        BoundsRecord r{};
+        CF_CUDA(u.take(&r));
+        if (!r.flag || !first) continue;
+        first = false;
+        if (found) *found = 1;
+        if (where && where_cap > 0) std::snprintf(where, (size_t)where_cap, "%s:%d", u.file, r.line);
+        if (index) *index = r.index;
+        if (limit) *limit = r.limit;
+    }
+    return CF_OK;
+}
+
+int cf_debug_force_bad_item(cf_world* w, const cf_step_params* p, int first)
+{
+#ifndef CF_DEBUG_BOUNDS
+    (void)w;
+    (void)p;
+    (void)first;
+    return fail(CF_ERR_INVALID, "cf_debug_force_bad_item needs the bounds-checked library");
+#else
+    int rc = check_world(w);
+    if (rc) return rc;
+    StepConsts c;
+    rc = prepare_step(w, p, &c);
+    if (!rc) rc = ensure_cells(w, c.grid.cells);
+    if (!rc) rc = ensure_plan(w, c.grid);
+    if (!rc) rc = ensure_offsets(w, c.grid.cells);
+    if (rc) return rc;
+    int which = 0;
+    rc = enqueue_cell_list(w, c, &which);
+    if (rc) return rc;
+    // the first item's first particle (Item::first, its first field) overwritten
+    CF_CUDA(cudaMemcpyAsync(w->s.items, &first, sizeof(int), cudaMemcpyHostToDevice, w->stream));
+    CF_CUDA(cudaStreamSynchronize(w->stream));
+    rc = enqueue_force(w, c, which);
+    if (rc) return rc;
+    return sync_and_check(w);
+#endif
 }
 
 int cf_work_counters(cf_world* w, const cf_step_params* p, uint64_t* c27, uint64_t* interacting)

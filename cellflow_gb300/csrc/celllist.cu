@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(kThreads)
     int cz = cell_coord(p.z, g.inv[2], g.m[2]);
     const uint32_t key = world * (uint32_t)g.cells_w + (uint32_t)((cz * g.m[1] + cy) * g.m[0] + cx);
     keys[i] = key;
+    if (!CF_IN_BOUNDS(key, g.cells)) return;
     const uint32_t s = atomicAdd(&counts[key], 1u);
     if (slot) slot[i] = s;
 }
@@ -412,10 +413,14 @@ __global__ void __launch_bounds__(kTileThreads)
 
 __global__ void __launch_bounds__(kThreads)
     place_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ slot,
-                 const uint32_t* __restrict__ cell_off, int n, uint32_t* __restrict__ unsorted)
+                 const uint32_t* __restrict__ cell_off, int n, int cells, uint32_t* __restrict__ unsorted)
 {
     const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (i < n) unsorted[cell_off[keys[i]] + slot[i]] = (uint32_t)i;
+    if (i >= n) return;
+    const uint32_t key = keys[i];
+    if (!CF_IN_BOUNDS(key, cells)) return;
+    const uint32_t dst = cell_off[key] + slot[i];
+    if (CF_IN_BOUNDS(dst, n)) unsorted[dst] = (uint32_t)i;
 }
 
 // Unordered cell list: particle i straight to offset[cell] + arrival slot,
@@ -423,14 +428,16 @@ __global__ void __launch_bounds__(kThreads)
 // within a cell).
 __global__ void __launch_bounds__(kThreads)
     place_gather_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ slot,
-                        const uint32_t* __restrict__ cell_off, const float4* __restrict__ pos, int n,
+                        const uint32_t* __restrict__ cell_off, const float4* __restrict__ pos, int n, int cells,
                         uint32_t* __restrict__ vals_sorted, uint32_t* __restrict__ keys_sorted,
                         float4* __restrict__ pos_sorted)
 {
     const int i = blockIdx.x * kThreads + threadIdx.x;
     if (i >= n) return;
     const uint32_t key = keys[i];
+    if (!CF_IN_BOUNDS(key, cells)) return;
     const uint32_t dst = cell_off[key] + slot[i];
+    if (!CF_IN_BOUNDS(dst, n)) return;
     vals_sorted[dst] = (uint32_t)i;
     keys_sorted[dst] = key;
     pos_sorted[dst] = pos[i];
@@ -442,17 +449,21 @@ constexpr uint32_t kRankWarpMin = 64;
 
 __global__ void __launch_bounds__(kThreads)
     rank_gather_kernel(const uint32_t* __restrict__ unsorted, const uint32_t* __restrict__ keys,
-                       const uint32_t* __restrict__ cell_off, const float4* __restrict__ pos, int n,
+                       const uint32_t* __restrict__ cell_off, const float4* __restrict__ pos, int n, int cells,
                        uint32_t* __restrict__ vals_sorted, uint32_t* __restrict__ keys_sorted,
                        float4* __restrict__ pos_sorted)
 {
     __shared__ uint32_t s_hist[kWarps][33];
     const int p = blockIdx.x * kThreads + threadIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const bool valid = p < n;
+    bool valid = p < n;
     uint32_t i = valid ? unsorted[p] : 0u;
-    const uint32_t key = valid ? keys[i] : 0xffffffffu;
-    const uint32_t b = valid ? cell_off[key] : 0u, e = valid ? cell_off[key + 1] : 0u;
+    valid = valid && CF_IN_BOUNDS(i, n);
+    uint32_t key = valid ? keys[i] : 0xffffffffu;
+    valid = valid && CF_IN_BOUNDS(key, cells);
+    uint32_t b = valid ? cell_off[key] : 0u, e = valid ? cell_off[key + 1] : 0u;
+    valid = valid && CF_IN_BOUNDS(e, n + 1) && b <= e;
+    if (!valid) key = 0xffffffffu;
     const uint32_t key0 = __shfl_sync(0xffffffffu, key, 0);
     if (__all_sync(0xffffffffu, valid && key == key0) && e - b > kRankWarpMin) {
         // The warp's 32 positions lie in one large cell [b, e).  Sort the warp's own
@@ -491,6 +502,7 @@ __global__ void __launch_bounds__(kThreads)
         }
         i = v;
         const uint32_t dst = b + rank;
+        if (!CF_IN_BOUNDS(i, n) || !CF_IN_BOUNDS(dst, n)) return;
         vals_sorted[dst] = i;
         keys_sorted[dst] = key;
         pos_sorted[dst] = pos[i];
@@ -500,6 +512,7 @@ __global__ void __launch_bounds__(kThreads)
     uint32_t rank = 0;
     for (uint32_t q = b; q < e; q++) rank += unsorted[q] < i ? 1u : 0u;
     const uint32_t dst = b + rank;
+    if (!CF_IN_BOUNDS(dst, n)) return;
     vals_sorted[dst] = i;
     keys_sorted[dst] = key;
     pos_sorted[dst] = pos[i];
@@ -580,6 +593,8 @@ constexpr int kSortItemsLarge = 16;
 inline int sort_items(int n) { return n <= (1 << 18) ? kSortItemsSmall : kSortItemsLarge; }
 
 }  // namespace
+
+CF_BOUNDS_READER(celllist)
 
 size_t radix_hist_entries(int n)
 {
@@ -746,14 +761,14 @@ cudaError_t launch_cell_list_csr(const float4* pos, int n, const Grid& g, const 
     note_launches(st);
     *which = 1;
     if (n > 0 && !stable) {
-        place_gather_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.keys[0], s.aux, cell_off, pos, n,
+        place_gather_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.keys[0], s.aux, cell_off, pos, n, g.cells,
                                                                           s.vals[1], s.keys[1], s.pos_sorted);
         note_launches(st);
     } else if (n > 0) {
-        place_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.keys[0], s.aux, cell_off, n, s.vals[0]);
+        place_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.keys[0], s.aux, cell_off, n, g.cells, s.vals[0]);
         note_launches(st);
         rank_gather_kernel<<<blocks_for(n, kThreads), kThreads, 0, st>>>(s.vals[0], s.keys[0], cell_off, pos, n,
-                                                                         s.vals[1], s.keys[1], s.pos_sorted);
+                                                                         g.cells, s.vals[1], s.keys[1], s.pos_sorted);
         note_launches(st);
     }
     return cudaGetLastError();

@@ -29,6 +29,63 @@ enum : int {
     kDevErrWait = 4,    // a bounded device wait gave up
 };
 
+// ---- bounds-checked build (compiled with -DCF_DEBUG_BOUNDS) -------------------
+//
+// Checked accesses test their index first; in the checked build an index
+// outside [0, limit) is recorded (the first one per translation unit, in a
+// device variable of that unit) and the access is skipped, so the kernel
+// carries on and the host reads the record (cf_debug_bounds).  In the normal
+// build the test compiles away.
+struct BoundsRecord {
+    int flag;  // 1: a violation was recorded
+    int line;  // source line of the check
+    long long index, limit;
+};
+#if defined(__CUDACC__)
+#ifdef CF_DEBUG_BOUNDS
+static __device__ BoundsRecord cf_bounds_rec;
+#endif
+__device__ __forceinline__ bool bounds_ok(long long idx, long long lim, int line)
+{
+#ifdef CF_DEBUG_BOUNDS
+    if (idx >= 0 && idx < lim) return true;
+    if (atomicCAS(&cf_bounds_rec.flag, 0, 1) == 0) {
+        cf_bounds_rec.line = line;
+        cf_bounds_rec.index = idx;
+        cf_bounds_rec.limit = lim;
+    }
+    return false;
+#else
+    (void)idx;
+    (void)lim;
+    (void)line;
+    return true;
+#endif
+}
+#define CF_IN_BOUNDS(idx, lim) ::cf::bounds_ok((long long)(idx), (long long)(lim), __LINE__)
+// The host reader of a unit's record (read and cleared); defined once per checked unit.
+#ifdef CF_DEBUG_BOUNDS
+#define CF_BOUNDS_READER(name)                                                               \
+    cudaError_t bounds_take_##name(BoundsRecord* out)                                        \
+    {                                                                                        \
+        cudaError_t e = cudaMemcpyFromSymbol(out, cf_bounds_rec, sizeof(BoundsRecord));      \
+        const BoundsRecord zero{};                                                           \
+        if (e == cudaSuccess) e = cudaMemcpyToSymbol(cf_bounds_rec, &zero, sizeof(zero));    \
+        return e;                                                                            \
+    }
+#else
+#define CF_BOUNDS_READER(name)                        \
+    cudaError_t bounds_take_##name(BoundsRecord* out) \
+    {                                                 \
+        *out = BoundsRecord{};                        \
+        return cudaSuccess;                           \
+    }
+#endif
+#endif
+cudaError_t bounds_take_celllist(BoundsRecord* out);
+cudaError_t bounds_take_step(BoundsRecord* out);
+cudaError_t bounds_take_proximity(BoundsRecord* out);
+
 // Tables padded to the maximum type count so any 5-bit type index stays in
 // bounds: index = (self & 31) * 32 + (other & 31).
 constexpr int kTableStride = CF_MAX_TYPES;

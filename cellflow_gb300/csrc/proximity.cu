@@ -148,11 +148,12 @@ __global__ void __launch_bounds__(kThreads)
     for (int t = (int)blockIdx.x * kSelWarps + (threadIdx.x >> 5); t < n; t += warps) {
         const float4 h = pos_sorted[t];
         const uint32_t i = vals_sorted[t];
+        const uint32_t key = keys_sorted[t];
+        if (!CF_IN_BOUNDS(i, n) || !CF_IN_BOUNDS(key, g.cells)) continue;  // (bounds-checked build)
         if (cap <= 0) {
             if (lane == 0) count[i] = 0;
             continue;
         }
-        const uint32_t key = keys_sorted[t];
         const int cx = (int)(key % (uint32_t)mx);
         const int cy = (int)((key / (uint32_t)mx) % (uint32_t)my);
         const int cz = (int)(key / (uint32_t)(mx * my));
@@ -167,6 +168,7 @@ __global__ void __launch_bounds__(kThreads)
             const uint32_t row = (uint32_t)((z * my + y) * mx);
             beg = cell_off[row + xlo];
             len = (int)(cell_off[row + xhi + 1] - beg);
+            if (!CF_IN_BOUNDS(len, n + 1) || !CF_IN_BOUNDS(beg + len, n + 1)) len = 0;
         }
         int incl = len;
 #pragma unroll
@@ -189,7 +191,7 @@ __global__ void __launch_bounds__(kThreads)
                 bool ok = false;
                 int cj = 0;
                 float cd = 0.0f;
-                if (gg < lim) {
+                if (gg < lim && CF_IN_BOUNDS(list[gg], n)) {
                     const uint32_t u = list[gg];
                     const float4 q = pos_sorted[u];
                     if (__float_as_uint(q.w) == __float_as_uint(h.w)) {
@@ -413,6 +415,8 @@ __global__ void __launch_bounds__(256)
 }
 
 }  // namespace
+
+CF_BOUNDS_READER(proximity)
 
 cudaError_t launch_mesh_select(const float4* pos_sorted, const uint32_t* keys_sorted, const uint32_t* vals_sorted,
                                const uint32_t* cell_start, const uint32_t* cell_end, const Grid& g, int n, float dsq,

@@ -231,6 +231,7 @@ __device__ __forceinline__ bool pair_test(const StepConsts& c, const Lane& L, co
     bool inter = d2 < (kUniformR ? c.thr_lo_uniform : tb.thr_lo[pair]);
     if (!inter) {
         // within rounding of the threshold: the reference's exact test
+        if (!CF_IN_BOUNDS(meta & kIndexMask, c.n)) return false;
         const float4 o = pos_sorted[meta & kIndexMask];
         float ex = __fsub_rn(o.x, L.h.x), ey = __fsub_rn(o.y, L.h.y), ez = __fsub_rn(o.z, L.h.z);
         if (kGeneric) {
@@ -332,6 +333,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     const float* xyf = reinterpret_cast<const float*>(w.xy);
     const float* zcf = reinterpret_cast<const float*>(w.zc);
     const Item it = items[item];
+    // (bounds-checked build) the item's particles lie in [0, n): else the item's warps skip it
+    if (!CF_IN_BOUNDS(it.count - 1, 32) || !CF_IN_BOUNDS(it.first, c.n) || !CF_IN_BOUNDS(it.first + it.count - 1, c.n))
+        return;
     const bool active = lane < it.count;
     const int t = it.first + (active ? lane : 0);
     Lane L;
@@ -434,10 +438,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
             } else if (half == 1) {
                 b = a - 1;
             }
-            if (row < ny * nz && b >= a) {
+            if (row < ny * nz && b >= a && CF_IN_BOUNDS(world_base + (uint32_t)((zz * my + yy) * mx) + b + 1,
+                                                        c.grid.cells + 1)) {
                 const uint32_t base = world_base + (uint32_t)((zz * my + yy) * mx);
                 seg_beg = (int)cell_off[base + a];
                 seg_len = (int)cell_off[base + b + 1] - seg_beg;
+                if (!CF_IN_BOUNDS(seg_len, c.n + 1) || !CF_IN_BOUNDS(seg_beg + seg_len, c.n + 1)) seg_len = 0;
                 if (!kGeneric) {
                     seg_sx = code_shift(cx, c.ext[0]) - ox;
                     seg_sy = code_shift(cy, c.ext[1]) - oy;
@@ -484,7 +490,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                 for (int g = lo + lane; g < hi; g += 32) {
                     const int slot = g - base;
                     const int j = beg + (g - pre);
-                    const float4 p = pos_sorted[j];
+                    const float4 p = CF_IN_BOUNDS(j, c.n) ? pos_sorted[j] : make_float4(kFar, kFar, kFar, 0.0f);
                     float* xy = reinterpret_cast<float*>(&w.xy[slot >> 1]);
                     float* zc = reinterpret_cast<float*>(&w.zc[slot >> 1]);
                     const float x = p.x + sx, y = p.y + sy, z = p.z + sz;
@@ -881,6 +887,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 
     // density-adaptive scale and integrator (ParticleSimulation.cu:136-161)
     const uint32_t i = vals_sorted[t];
+    if (!CF_IN_BOUNDS(i, c.n)) return;
     const int prev = counts[i];
     const float avg = __fmul_rn((float)(L.count + prev), 0.5f);
     const float density = fminf(__fdiv_rn(avg, (float)c.max_expected_neighbors), 1.0f);
@@ -1055,6 +1062,8 @@ cudaError_t launch_variant(const StepConsts& c, const PairTables* tables, const 
 }
 
 }  // namespace
+
+CF_BOUNDS_READER(step)
 
 cudaError_t launch_force_work(const StepConsts& c, const uint32_t* keys_sorted, const uint32_t* cell_off,
                               const Item* items, const int* n_items, int max_items, unsigned long long* out,

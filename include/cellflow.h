@@ -278,6 +278,21 @@ int cf_work_counters(cf_world* w, const cf_step_params* p, uint64_t* c27, uint64
  * cell list; the particle state is unchanged. */
 int cf_force_work(cf_world* w, const cf_step_params* p, uint64_t* staged, uint64_t* tested);
 
+/* Bounds-checked library (libcellflow_bounds.so, built with -DCF_DEBUG_BOUNDS;
+ * no counterpart in the reference, whose kernels had no index checks).  The
+ * cell-list, force and proximity kernels test their derived indices before
+ * each access; an index outside its buffer is recorded (the first per source
+ * file) and the access skipped, instead of faulting.  cf_debug_bounds reports
+ * whether this library is the checked one, and the first recorded violation
+ * ("file.cu:line", the index and its limit), then clears the records.  In the
+ * normal library checked = 0 and nothing is ever found. */
+int cf_debug_bounds(int* checked, int* found, char* where, int where_cap, long long* index, long long* limit);
+/* Checked library only (else CF_ERR_INVALID): builds the step's cell list,
+ * overwrites the first force-kernel item's first particle with `first`, and
+ * runs the force kernel: a first outside [0, n) must be recorded by
+ * cf_debug_bounds and that item skipped.  The other items are stepped. */
+int cf_debug_force_bad_item(cf_world* w, const cf_step_params* p, int first);
+
 /* ---- proximity graph ---------------------------------------------------- */
 
 /* generateProximityGraph (ParticleSimulation.cu:625-687, kernel :188-277) with

@@ -39,6 +39,18 @@ def test_library_exports_every_declared_symbol(cflib):
         assert hasattr(cflib, name)
 
 
+def test_bounds_build_exports_the_same_symbols():
+    """The bounds-checked library (-DCF_DEBUG_BOUNDS) builds and exports every declared function."""
+    from cellflow_gb300 import build
+
+    lib = build.build(bounds=True)
+    exported = subprocess.run(["nm", "-D", "--defined-only", str(lib)], capture_output=True, text=True,
+                              check=True).stdout
+    symbols = {line.split()[-1] for line in exported.splitlines() if line.strip()}
+    missing = declared_functions() - symbols
+    assert not missing, f"declared but not exported: {sorted(missing)}"
+
+
 def test_binding_covers_header(cflib):
     from cellflow_gb300 import _lib
 
