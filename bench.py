@@ -368,9 +368,10 @@ def run_gb300(args, rank, world, local, name, steps, warmup, cpu_seconds, extras
         if world > 1:
             torch.distributed.barrier()
 
-    force_variant = sim.autotune(params, 5)  # picks the force-kernel variant; restores the state
     for _ in range(warmup):
         sim.simulate(params, 1)
+    # picks the force-kernel variant on the state the timed steps start from; restores the state
+    force_variant = sim.autotune(params, 5)
     sim.sync()
     state0 = sim.get_state()
 
