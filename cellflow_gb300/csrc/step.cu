@@ -219,6 +219,42 @@ __device__ __forceinline__ void staged_delta(const StepConsts& c, float cx, floa
 // fallback.  Returns the staged displacement and its contracted d^2.
 // `origin` is the pass's staging origin (unused on generic grids).
 template <bool kGeneric, bool kUniformR>
+__device__ __forceinline__ bool pair_fast(const StepConsts& c, const Lane& L, const HomeOps& H, float cx, float cy,
+                                          float cz, uint32_t meta, const Tables& tb, float& dx, float& dy, float& dz,
+                                          float& d2)
+{
+    staged_delta<kGeneric>(c, cx, cy, cz, L.h, H, dx, dy, dz);
+    d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const uint32_t other = meta >> kTypeShift;
+    const uint32_t pair = L.tp * kTableStride + other;
+    return d2 < (kUniformR ? c.thr_lo_uniform : tb.thr_lo[pair]);
+}
+
+// The reference's exact test for a pair the certain-interaction bound left
+// open (within rounding of the threshold), on the unshifted coordinates.
+template <bool kGeneric, bool kUniformR>
+__device__ __forceinline__ bool pair_exact(const StepConsts& c, const Lane& L, const float* origin, float cx, float cy,
+                                           float cz, uint32_t meta, const float4* __restrict__ pos_sorted,
+                                           const Tables& tb)
+{
+    if (!CF_IN_BOUNDS(meta & kIndexMask, c.n)) return false;
+    const float4 o = pos_sorted[meta & kIndexMask];
+    float ex = __fsub_rn(o.x, L.h.x), ey = __fsub_rn(o.y, L.h.y), ez = __fsub_rn(o.z, L.h.z);
+    if (kGeneric) {
+        ex = wrap_ref(ex, c.ext[0], c.half[0]);
+        ey = wrap_ref(ey, c.ext[1], c.half[1]);
+        ez = wrap_ref(ez, c.ext[2], c.half[2]);
+    } else {
+        ex = __fadd_rn(ex, staged_shift(cx + origin[0], o.x, c.ext[0]));
+        ey = __fadd_rn(ey, staged_shift(cy + origin[1], o.y, c.ext[1]));
+        ez = __fadd_rn(ez, staged_shift(cz + origin[2], o.z, c.ext[2]));
+    }
+    const float e2 = __fadd_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), __fmul_rn(ez, ez));
+    const uint32_t pair = L.tp * kTableStride + (meta >> kTypeShift);
+    return __fadd_rn(e2, 0.0001f) < (kUniformR ? c.thr_uniform : tb.thr[pair]);
+}
+
+template <bool kGeneric, bool kUniformR>
 __device__ __forceinline__ bool pair_test(const StepConsts& c, const Lane& L, const HomeOps& H,
                                           const float* origin, float cx, float cy, float cz, uint32_t meta,
                                           const float4* __restrict__ pos_sorted, const Tables& tb, float& dx,
@@ -799,7 +835,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                         upto = kPer * it + fw;
                     }
                 }
-                if (kPer * it < upto) {
+                // every lane runs the trip (a lane whose pairs are done has none valid), so the
+                // warp-wide vote below is reached by all 32 lanes in every trip
+                {
                     int slot[kPer];
                     bool valid[kPer];
 #pragma unroll
@@ -810,20 +848,31 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                             gi = __ffs(nz) - 1;  // a later group holds a hit
                             m = w.mask[gi * 32 + src];
                         }
-                        slot[q] = valid[q] ? gi * 32 + (__ffs(m) - 1) : slot[0];
+                        slot[q] = valid[q] ? gi * 32 + (__ffs(m) - 1) : (q == 0 ? 0 : slot[0]);
                         if (valid[q]) m &= m - 1u;
                     }
                     float dx[kPer], dy[kPer], dz[kPer], d2[kPer], wgt[kPer];
                     uint32_t meta[kPer];
                     bool inter[kPer];
+                    float sx[kPer], sy[kPer], sz[kPer];
+                    bool band = false;
 #pragma unroll
                     for (int q = 0; q < kPer; q++) {
-                        float x, y, z;
-                        staged_xyz(xyf, zcf, slot[q], x, y, z);
+                        staged_xyz(xyf, zcf, slot[q], sx[q], sy[q], sz[q]);
                         meta[q] = w.meta[slot[q]];
-                        inter[q] = pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta[q], pos_sorted, tb,
-                                                                  dx[q], dy[q], dz[q], d2[q]) &&
-                                   valid[q];
+                        const bool fast = pair_fast<kGeneric, kUniformR>(c, L, H, sx[q], sy[q], sz[q], meta[q], tb,
+                                                                        dx[q], dy[q], dz[q], d2[q]);
+                        inter[q] = fast && valid[q];
+                        band |= valid[q] && !fast;
+                    }
+                    // pairs within rounding of the threshold are rare: the exact test runs only in
+                    // the trips where some lane of the warp holds one
+                    if (__any_sync(0xffffffffu, band)) {
+#pragma unroll
+                        for (int q = 0; q < kPer; q++)
+                            if (valid[q] && !inter[q])
+                                inter[q] = pair_exact<kGeneric, kUniformR>(c, L, w.origin, sx[q], sy[q], sz[q],
+                                                                           meta[q], pos_sorted, tb);
                     }
 #pragma unroll
                     for (int q = 0; q < kPer; q++) wgt[q] = pair_weight<kUniformR>(d2[q], meta[q], L, tb, c1u);
