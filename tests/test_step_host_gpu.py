@@ -1,6 +1,7 @@
 """cf_step_host (one step from and to host records) equals cf_set_particles + cf_step +
-cf_get_particles bit for bit, with page-locked buffers (one CUDA graph) and pageable ones
-(the three calls), and reports a position outside the box like the separate calls."""
+cf_get_particles bit for bit, with page-locked buffers (one CUDA graph; aligned and not)
+and pageable ones (the three calls), and reports a position outside the box like the
+separate calls."""
 
 import numpy as np
 import pytest
@@ -20,22 +21,26 @@ def world(w):
     return sim
 
 
-def pinned_records(n):
+def pinned_records(n, offset=0):
+    """Page-locked 44-B records starting `offset` bytes into a page-locked allocation."""
     import torch
 
-    buf = torch.empty(n * PARTICLE_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
-    return buf, buf.numpy().view(PARTICLE_DTYPE)
+    buf = torch.empty(n * PARTICLE_DTYPE.itemsize + 16, dtype=torch.uint8).pin_memory()
+    return buf, buf.numpy()[offset:offset + n * PARTICLE_DTYPE.itemsize].view(PARTICLE_DTYPE)
 
 
-@pytest.mark.parametrize("pinned", [True, False])
-def test_step_host_equals_the_three_calls(cflib, pinned):
-    w = inputs.Workload("host", n=20000, num_types=5, radius=0.1, steps=1, seed=31)
+# page-locked records are read and written in place word by word, at any 4-B aligned
+# start (offset 4) and any count; pageable ones go through the three calls
+@pytest.mark.parametrize("n,pinned,offset", [(20000, True, 0), (10240, True, 0), (20000, True, 4),
+                                             (20000, False, 0)])
+def test_step_host_equals_the_three_calls(cflib, n, pinned, offset):
+    w = inputs.Workload("host", n=n, num_types=5, radius=0.1, steps=1, seed=31)
     params = w.params()
     a, b = world(w), world(w)
     rec = a.getParticleData()
     keep = None
     if pinned:
-        keep, io = pinned_records(w.n)
+        keep, io = pinned_records(w.n, offset)
         io[:] = rec
     else:
         io = rec.copy()
