@@ -21,6 +21,15 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kMaxHeld = 2 * CF_MAX_PROX_CONN;
 
+// A particle's cell along one axis, computed from its position exactly as the
+// cell list's hash computed it (three multiplies instead of dividing the cell
+// id back into coordinates).
+__device__ __forceinline__ int axis_cell(float x, float inv, int m)
+{
+    const int c = __float2int_rd(__fmul_rn(x, inv));
+    return min(max(c, 0), m - 1);
+}
+
 // Calls fn(u) for every sorted slot u in the cells within one cell of (cx, cy,
 // cz), clipped at the box (the proximity grid is not periodic), in cell order.
 // kCsr: cell_start = CSR offsets, cell_end = offsets + 1, so each of the
@@ -69,9 +78,10 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t i = vals_sorted[t];
     const uint32_t key = keys_sorted[t];
     const int mx = g.m[0], my = g.m[1], mz = g.m[2];
-    const int cx = (int)(key % (uint32_t)mx);
-    const int cy = (int)((key / (uint32_t)mx) % (uint32_t)my);
-    const int cz = (int)(key / (uint32_t)(mx * my));
+    const int cx = axis_cell(h.x, g.inv[0], mx);
+    const int cy = axis_cell(h.y, g.inv[1], my);
+    const int cz = axis_cell(h.z, g.inv[2], mz);
+    (void)key;
     const int cap = 2 * max_conn;
     if (cap <= 0) {
         count[i] = 0;
@@ -154,9 +164,9 @@ __global__ void __launch_bounds__(kThreads)
             if (lane == 0) count[i] = 0;
             continue;
         }
-        const int cx = (int)(key % (uint32_t)mx);
-        const int cy = (int)((key / (uint32_t)mx) % (uint32_t)my);
-        const int cz = (int)(key / (uint32_t)(mx * my));
+        const int cx = axis_cell(h.x, g.inv[0], mx);
+        const int cy = axis_cell(h.y, g.inv[1], my);
+        const int cz = axis_cell(h.z, g.inv[2], mz);
         const int xlo = max(cx - 1, 0), xhi = min(cx + 1, mx - 1);
         const int ylo = max(cy - 1, 0), yhi = min(cy + 1, my - 1);
         const int zlo = max(cz - 1, 0), zhi = min(cz + 1, mz - 1);
@@ -309,9 +319,10 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t i = vals_sorted[t];
     const uint32_t key = keys_sorted[t];
     const int mx = g.m[0], my = g.m[1], mz = g.m[2];
-    const int cx = (int)(key % (uint32_t)mx);
-    const int cy = (int)((key / (uint32_t)mx) % (uint32_t)my);
-    const int cz = (int)(key / (uint32_t)(mx * my));
+    const int cx = axis_cell(h.x, g.inv[0], mx);
+    const int cy = axis_cell(h.y, g.inv[1], my);
+    const int cz = axis_cell(h.z, g.inv[2], mz);
+    (void)key;
     const int cap = min(max_conn, kMeshHeld);
     int held = 0;
     int hj[kMeshHeld];
