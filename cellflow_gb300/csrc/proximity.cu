@@ -174,7 +174,9 @@ __global__ void __launch_bounds__(kThreads)
         uint32_t beg = 0u;
         int len = 0;
         if (lane < nrows) {
-            const int y = ylo + lane % ny, z = zlo + lane / ny;
+            // lane / ny for lane < 9 and ny in {1, 2, 3} without a division: (lane * 11) >> 5 = lane / 3
+            const int zq = ny == 3 ? (lane * 11) >> 5 : (ny == 2 ? lane >> 1 : lane);
+            const int y = ylo + (lane - zq * ny), z = zlo + zq;
             const uint32_t row = (uint32_t)((z * my + y) * mx);
             beg = cell_off[row + xlo];
             len = (int)(cell_off[row + xhi + 1] - beg);
