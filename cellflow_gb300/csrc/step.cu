@@ -705,14 +705,24 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                     float dx[kPer], dy[kPer], dz[kPer], d2[kPer], wgt[kPer];
                     uint32_t meta[kPer];
                     bool inter[kPer];
+                    // (every lane runs this body in every pass of the loop, so the vote is warp-wide)
+                    float sx[kPer], sy[kPer], sz[kPer];
+                    bool band = false;
 #pragma unroll
                     for (int q = 0; q < kPer; q++) {
-                        float x, y, z;
-                        staged_xyz(xyf, zcf, slot[q], x, y, z);
+                        staged_xyz(xyf, zcf, slot[q], sx[q], sy[q], sz[q]);
                         meta[q] = w.meta[slot[q]];
-                        inter[q] = valid[q] && pair_test<kGeneric, kUniformR>(c, L, H, w.origin, x, y, z, meta[q],
-                                                                              pos_sorted, tb, dx[q], dy[q], dz[q],
-                                                                              d2[q]);
+                        const bool fast = pair_fast<kGeneric, kUniformR>(c, L, H, sx[q], sy[q], sz[q], meta[q], tb,
+                                                                        dx[q], dy[q], dz[q], d2[q]);
+                        inter[q] = fast && valid[q];
+                        band |= valid[q] && !fast;
+                    }
+                    if (__any_sync(0xffffffffu, band)) {
+#pragma unroll
+                        for (int q = 0; q < kPer; q++)
+                            if (valid[q] && !inter[q])
+                                inter[q] = pair_exact<kGeneric, kUniformR>(c, L, w.origin, sx[q], sy[q], sz[q],
+                                                                           meta[q], pos_sorted, tb);
                     }
 #pragma unroll
                     for (int q = 0; q < kPer; q++) wgt[q] = pair_weight<kUniformR>(d2[q], meta[q], L, tb, c1u);
