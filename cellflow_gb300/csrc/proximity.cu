@@ -76,12 +76,10 @@ __global__ void __launch_bounds__(kThreads)
     if (t >= n) return;
     const float4 h = pos_sorted[t];
     const uint32_t i = vals_sorted[t];
-    const uint32_t key = keys_sorted[t];
     const int mx = g.m[0], my = g.m[1], mz = g.m[2];
     const int cx = axis_cell(h.x, g.inv[0], mx);
     const int cy = axis_cell(h.y, g.inv[1], my);
     const int cz = axis_cell(h.z, g.inv[2], mz);
-    (void)key;
     const int cap = 2 * max_conn;
     if (cap <= 0) {
         count[i] = 0;
@@ -319,12 +317,10 @@ __global__ void __launch_bounds__(kThreads)
     if (t >= n) return;
     const float4 h = pos_sorted[t];
     const uint32_t i = vals_sorted[t];
-    const uint32_t key = keys_sorted[t];
     const int mx = g.m[0], my = g.m[1], mz = g.m[2];
     const int cx = axis_cell(h.x, g.inv[0], mx);
     const int cy = axis_cell(h.y, g.inv[1], my);
     const int cz = axis_cell(h.z, g.inv[2], mz);
-    (void)key;
     const int cap = min(max_conn, kMeshHeld);
     int held = 0;
     int hj[kMeshHeld];
