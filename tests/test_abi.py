@@ -66,6 +66,13 @@ def test_host_only_calls_without_gpu(cflib):
     assert abs(p.radius - 42.07) < 1e-5 and p.num_particle_types == 6 and p.max_expected_neighbors == 400
     assert cflib.cf_version().startswith(b"cellflow-gb300")
     assert cflib.cf_lfo_ratio(0.5, 0.0, 0.1, 3.0) == pytest.approx(0.5)
+    # the normal library reports itself unchecked, with nothing recorded
+    import ctypes as C
+
+    checked, found = C.c_int(7), C.c_int(7)
+    where = C.create_string_buffer(b"x" * 16)
+    assert cflib.cf_debug_bounds(C.byref(checked), C.byref(found), where, 16, None, None) == 0
+    assert checked.value == 0 and found.value == 0 and where.value == b""
 
 
 def test_lfo_matches_oracle(cflib):
