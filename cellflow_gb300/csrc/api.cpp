@@ -1768,12 +1768,15 @@ namespace {
 // reallocations drop it), or directly when graphs are off.
 extern "C++" {
 template <typename Body>
-int run_selection(cf_world* w, int kind, const Grid& g, float dsq, int max_conn, Body body)
+int run_selection(cf_world* w, int kind, const Grid& g, float dsq, int max_conn, Body body, const void* out = nullptr,
+                  long long out_cap = -1, const ColorTable* colors = nullptr)
 {
     if (!w->use_graphs || w->stream == nullptr) return body();
     SelGraph& sg = w->sel_graph[kind];
+    const ColorTable ct = colors ? *colors : ColorTable{};
     if (!(sg.exec && std::memcmp(&sg.g, &g, sizeof(g)) == 0 && sg.dsq == dsq && sg.max_conn == max_conn &&
-          sg.n == w->n && sg.types == w->num_types)) {
+          sg.n == w->n && sg.types == w->num_types && sg.out == out && sg.out_cap == out_cap &&
+          std::memcmp(&sg.colors, &ct, sizeof(ct)) == 0)) {
         if (sg.exec) cudaGraphExecDestroy(sg.exec);
         sg = SelGraph();
         cudaGraph_t graph = nullptr;
@@ -1794,6 +1797,9 @@ int run_selection(cf_world* w, int kind, const Grid& g, float dsq, int max_conn,
         sg.max_conn = max_conn;
         sg.n = w->n;
         sg.types = w->num_types;
+        sg.out = out;
+        sg.out_cap = out_cap;
+        sg.colors = ct;
     }
     CF_CUDA(cudaGraphLaunch(sg.exec, w->stream));
     note_launches(w->stream, sg.kernels);
@@ -1954,19 +1960,42 @@ int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, cons
     if (rc) return rc;
     if (!colors || n_colors < w->num_types) return fail(CF_ERR_INVALID, "need one colour per type");
     if (cap_vertices < 0 || (cap_vertices > 0 && !vertices)) return fail(CF_ERR_INVALID, "bad vertex buffer");
-    rc = proximity_enqueue(w, distance, max_conn);
+    if (!(distance >= 0.0f) || !std::isfinite(distance)) return fail(CF_ERR_INVALID, "distance must be finite, >= 0");
+    if (max_conn < 0 || max_conn > CF_MAX_PROX_CONN)
+        return fail(CF_ERR_INVALID, "max_conn must be in [0, 16] (the reference overflowed its buffer above 16)");
+    rc = ensure_prox(w);
     if (rc) return rc;
-    if (cap_vertices > 0) {
-        // ParticleSimulation.cu:253 indexes colours by type % numParticleTypes
-        CF_CUDA(launch_proximity_emit_vertices(w->s.prox_slots, w->s.prox_count, w->n, max_conn, w->pos,
-                                               color_table(w, colors), w->num_types, vertices, cap_vertices,
-                                               w->stream));
-    }
+    Grid g = choose_prox_grid(w->ext, distance, kMaxCells);
+    rc = ensure_offsets(w, g.cells);
+    if (rc) return rc;
+    Scratch& s = w->s;
+    const float dsq = distance * distance;  // ParticleSimulation.cu:660
+    // ParticleSimulation.cu:253 indexes colours by type % numParticleTypes
+    const ColorTable ct = color_table(w, colors);
+    // one pass: the selection writes each particle's line vertices at places reserved by
+    // one atomic per particle (arbitrary order, as the reference's atomicAdd append,
+    // ParticleSimulation.cu:250); the edge total is read back
+    uint32_t* total = s.prox_count + w->n;
+    rc = run_selection(
+        w, 2, g, dsq, max_conn,
+        [&]() -> int {
+            int which = 0;
+            CF_CUDA(launch_cell_list_csr(w->pos, w->n, g, w->ext, w->num_types, s, s.cell_off, nullptr, nullptr,
+                                         w->err, &which, w->stream, false));
+            CF_CUDA(cudaMemsetAsync(total, 0, sizeof(uint32_t), w->stream));
+            CF_CUDA(launch_proximity_select_vertices(s.pos_sorted, s.keys[which], s.vals[which], s.cell_off, g, w->n,
+                                                     dsq, max_conn, w->pos, ct, w->num_types, vertices, cap_vertices,
+                                                     total, w->stream));
+            CF_CUDA(cudaMemcpyAsync(&w->host_words[1], total, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+            return CF_OK;
+        },
+        vertices, cap_vertices, &ct);
+    if (rc) return rc;
     rc = sync_and_check(w);
     if (rc) return rc;
-    const uint32_t total = (uint32_t)w->host_words[1];
-    if (vertex_count) *vertex_count = (int)(2 * total);
-    if (2 * (size_t)total > (size_t)cap_vertices) return fail(CF_ERR_CAPACITY, "vertex buffer too small");
+    const uint32_t edges = (uint32_t)w->host_words[1];
+    if (vertex_count) *vertex_count = (int)(2 * edges);
+    if (2 * (size_t)edges > (size_t)cap_vertices) return fail(CF_ERR_CAPACITY, "vertex buffer too small");
     return CF_OK;
 }
 

@@ -256,12 +256,21 @@ constexpr int kGradAccEntries = kTableSize + 8;
 
 // A cached CUDA graph of a selection pass (0: proximity edges, 1: triangle
 // mesh): cell list on its grid, selection kernel, scan, count read-back.
+// Per-type colours (r, g, b), passed to the emit kernels by value.
+struct ColorTable {
+    float c[3 * CF_MAX_TYPES];
+};
+
 struct SelGraph {
     cudaGraphExec_t exec = nullptr;
     long long kernels = 0;  // kernel nodes of exec
     Grid g{};
     float dsq = 0.0f;
     int max_conn = -1, n = -1, types = -1;
+    // the vertex-emitting selection: its output buffer and colours
+    const void* out = nullptr;
+    long long out_cap = -1;
+    ColorTable colors{};
 };
 
 }  // namespace cf
@@ -333,7 +342,7 @@ struct cf_world {
     const void* host_in = nullptr;
     void* host_out = nullptr;
     const void* host_bufs = nullptr;
-    cf::SelGraph sel_graph[2];
+    cf::SelGraph sel_graph[3];  // proximity (counts + scan), triangle mesh, proximity vertices
 };
 
 namespace cf {
@@ -408,18 +417,19 @@ cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* ke
 cudaError_t launch_mesh_select(const float4* pos_sorted, const uint32_t* keys_sorted, const uint32_t* vals_sorted,
                                const uint32_t* cell_start, const uint32_t* cell_end, const Grid& g, int n, float dsq,
                                int max_conn, int32_t* slots, uint32_t* count, cudaStream_t st);
-// Per-type colours (r, g, b), passed to the emit kernels by value.
-struct ColorTable {
-    float c[3 * CF_MAX_TYPES];
-};
 cudaError_t launch_mesh_emit(const int32_t* slots, const uint32_t* offsets, int n, const float4* pos,
                              const ColorTable& colors, int n_colors, int32_t* tris, float* vertices, long long cap_tris,
                              cudaStream_t st);
 cudaError_t launch_proximity_emit_edges(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,
                                         int32_t* edges, int cap, cudaStream_t st);
-cudaError_t launch_proximity_emit_vertices(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,
-                                           const float4* pos, const ColorTable& colors, int n_colors,
-                                           float* vertices, int cap_vertices, cudaStream_t st);
+// The CSR selection that writes each particle's line vertices itself, at an
+// offset reserved by one atomic per particle (vertex order is arbitrary, as the
+// reference's atomicAdd append); *total = edges found (zero on entry).
+cudaError_t launch_proximity_select_vertices(const float4* pos_sorted, const uint32_t* keys_sorted,
+                                             const uint32_t* vals_sorted, const uint32_t* cell_off, const Grid& g,
+                                             int n, float dsq, int max_conn, const float4* pos,
+                                             const ColorTable& colors, int n_colors, float* vertices,
+                                             int cap_vertices, uint32_t* total, cudaStream_t st);
 cudaError_t launch_init_particles(float4* pos, float4* vel, float4* acc, int* counts, int n, int num_types,
                                   const float* lo, const float* span, uint64_t seed, cudaStream_t st,
                                   uint32_t world = 0);

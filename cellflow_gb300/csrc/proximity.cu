@@ -8,9 +8,11 @@
 //
 // Here each particle scans only the cells within the distance and keeps the
 // 2*maxConn smallest qualifying indices, which is the same candidate set;
-// the same stable sort by squared distance then picks the same edges.  Edges
-// are placed by an exclusive scan of per-particle counts, so the output order
-// is deterministic: by i, then by distance.
+// the same stable sort by squared distance then picks the same edges.  For
+// the edge list, edges are placed by an exclusive scan of per-particle counts,
+// so its order is deterministic: by i, then by distance.  The line vertices
+// are written by the selection pass itself at places reserved by one atomic
+// per particle: arbitrary order, as the reference's append.
 #include <cuda_runtime.h>
 
 #include "cf_internal.hpp"
@@ -141,11 +143,17 @@ __global__ void __launch_bounds__(kThreads)
 constexpr int kSelWarps = kThreads / 32;
 constexpr int kSelListCap = 256;
 
+// kEmit: instead of the per-particle slots and counts, each particle's warp
+// reserves its edges' places with one atomic on *count (the running total) and
+// writes their line vertices itself (ParticleSimulation.cu:253-275: per edge the
+// vertex of i then of j, each x, y, z, r, g, b with the colour of i's type).
+template <bool kEmit>
 __global__ void __launch_bounds__(kThreads)
     proximity_select_warp_kernel(const float4* __restrict__ pos_sorted, const uint32_t* __restrict__ keys_sorted,
                                  const uint32_t* __restrict__ vals_sorted, const uint32_t* __restrict__ cell_off,
                                  Grid g, int n, float dsq, int max_conn, int32_t* __restrict__ slots,
-                                 uint32_t* __restrict__ count)
+                                 uint32_t* __restrict__ count, const float4* __restrict__ pos, ColorTable colors,
+                                 int n_colors, float* __restrict__ vertices, int cap_vertices)
 {
     __shared__ uint32_t s_list[kSelWarps][kSelListCap];
     const int lane = threadIdx.x & 31;
@@ -159,7 +167,7 @@ __global__ void __launch_bounds__(kThreads)
         const uint32_t key = keys_sorted[t];
         if (!CF_IN_BOUNDS(i, n) || !CF_IN_BOUNDS(key, g.cells)) continue;  // (bounds-checked build)
         if (cap <= 0) {
-            if (lane == 0) count[i] = 0;
+            if (!kEmit && lane == 0) count[i] = 0;
             continue;
         }
         const int cx = axis_cell(h.x, g.inv[0], mx);
@@ -247,8 +255,26 @@ __global__ void __launch_bounds__(kThreads)
             rank += (od < hd || (od == hd && oj < hj)) ? 1 : 0;
         }
         const int emit = min(held, max_conn);
-        if (lane < held && rank < emit) slots[(size_t)i * CF_MAX_PROX_CONN + rank] = hj;
-        if (lane == 0) count[i] = (uint32_t)emit;
+        if constexpr (kEmit) {
+            uint32_t base = 0u;
+            if (lane == 0 && emit > 0) base = atomicAdd(count, (uint32_t)emit);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (lane < held && rank < emit && CF_IN_BOUNDS(hj, n)) {
+                const size_t k = (size_t)base + (size_t)rank;
+                if (2 * k + 1 < (size_t)cap_vertices) {
+                    // ParticleSimulation.cu:253-275: i then j, each x, y, z, r, g, b with i's colour
+                    const float4 q = pos[hj];
+                    const uint32_t c = (__float_as_uint(h.w) & kTypeMask) % (uint32_t)n_colors;
+                    const float r = colors.c[3 * c], gg = colors.c[3 * c + 1], b = colors.c[3 * c + 2];
+                    float* v = vertices + k * 12;
+                    v[0] = h.x; v[1] = h.y; v[2] = h.z; v[3] = r; v[4] = gg; v[5] = b;
+                    v[6] = q.x; v[7] = q.y; v[8] = q.z; v[9] = r; v[10] = gg; v[11] = b;
+                }
+            }
+        } else {
+            if (lane < held && rank < emit) slots[(size_t)i * CF_MAX_PROX_CONN + rank] = hj;
+            if (lane == 0) count[i] = (uint32_t)emit;
+        }
     }
 }
 
@@ -265,31 +291,6 @@ __global__ void __launch_bounds__(256)
             edges[2 * (size_t)k] = i;
             edges[2 * (size_t)k + 1] = slots[(size_t)i * CF_MAX_PROX_CONN + e];
         }
-    }
-}
-
-// Line vertices in the reference's layout (ParticleSimulation.cu:253-275):
-// per edge, vertex of i then vertex of j, each x, y, z, r, g, b with the
-// colour of i's type.
-__global__ void __launch_bounds__(256)
-    proximity_vertices_kernel(const int32_t* __restrict__ slots, const uint32_t* __restrict__ offsets, int n,
-                              const float4* __restrict__ pos, ColorTable colors, int n_colors,
-                              float* __restrict__ vertices, int cap_vertices)
-{
-    const int i = blockIdx.x * 256 + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t o = offsets[i], e_count = offsets[i + 1] - o;
-    if (e_count == 0) return;
-    const float4 a = pos[i];
-    const uint32_t c = (__float_as_uint(a.w) & kTypeMask) % (uint32_t)n_colors;
-    const float r = colors.c[3 * c], gg = colors.c[3 * c + 1], b = colors.c[3 * c + 2];
-    for (uint32_t e = 0; e < e_count; e++) {
-        const uint32_t k = o + e;
-        if (2 * (size_t)k + 1 >= (size_t)cap_vertices) break;
-        const float4 q = pos[slots[(size_t)i * CF_MAX_PROX_CONN + e]];
-        float* v = vertices + (size_t)k * 12;
-        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = r; v[4] = gg; v[5] = b;
-        v[6] = q.x; v[7] = q.y; v[8] = q.z; v[9] = r; v[10] = gg; v[11] = b;
     }
 }
 
@@ -462,14 +463,31 @@ cudaError_t launch_proximity_select(const float4* pos_sorted, const uint32_t* ke
         // faster than a thread per particle, which wins only on near-uniform ones (0.081 against
         // 0.093 ms per call at 100k)
         const int warp_blocks = (n + kSelWarps - 1) / kSelWarps;
-        proximity_select_warp_kernel<<<warp_blocks, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted,
-                                                                      cell_start, g, n, dsq, max_conn, slots, count);
+        proximity_select_warp_kernel<false><<<warp_blocks, kThreads, 0, st>>>(
+            pos_sorted, keys_sorted, vals_sorted, cell_start, g, n, dsq, max_conn, slots, count, nullptr,
+            ColorTable{}, 1, nullptr, 0);
         note_launches(st);
     } else {
         proximity_select_kernel<false><<<blocks, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted, cell_start,
                                                                    cell_end, g, n, dsq, max_conn, slots, count);
         note_launches(st);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_proximity_select_vertices(const float4* pos_sorted, const uint32_t* keys_sorted,
+                                             const uint32_t* vals_sorted, const uint32_t* cell_off, const Grid& g,
+                                             int n, float dsq, int max_conn, const float4* pos,
+                                             const ColorTable& colors, int n_colors, float* vertices,
+                                             int cap_vertices, uint32_t* total, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    const int warp_blocks = (n + kSelWarps - 1) / kSelWarps;
+    proximity_select_warp_kernel<true><<<warp_blocks, kThreads, 0, st>>>(pos_sorted, keys_sorted, vals_sorted,
+                                                                         cell_off, g, n, dsq, max_conn, nullptr,
+                                                                         total, pos, colors, n_colors, vertices,
+                                                                         cap_vertices);
+    note_launches(st);
     return cudaGetLastError();
 }
 
@@ -483,16 +501,5 @@ cudaError_t launch_proximity_emit_edges(const int32_t* slots, const uint32_t* of
     return cudaGetLastError();
 }
 
-cudaError_t launch_proximity_emit_vertices(const int32_t* slots, const uint32_t* offsets, int n, int max_conn,
-                                           const float4* pos, const ColorTable& colors, int n_colors,
-                                           float* vertices, int cap_vertices, cudaStream_t st)
-{
-    (void)max_conn;
-    if (n <= 0 || cap_vertices <= 0) return cudaSuccess;
-    proximity_vertices_kernel<<<(n + 255) / 256, 256, 0, st>>>(slots, offsets, n, pos, colors, n_colors, vertices,
-                                                               cap_vertices);
-    note_launches(st);
-    return cudaGetLastError();
-}
 
 }  // namespace cf

@@ -307,7 +307,10 @@ int cf_proximity_edges(cf_world* w, float distance, int max_conn, int32_t* edges
 /* Same edge set, written as the reference's line vertices: per edge two
  * vertices of 6 floats (x, y, z, r, g, b), colour of particle i's type
  * (colors[type % T]).  `vertices` is a DEVICE buffer of cap_vertices*6
- * floats standing in for the GL VBO; *vertex_count = 2 * edges. */
+ * floats standing in for the GL VBO; *vertex_count = 2 * edges.  The edges'
+ * order in the buffer is arbitrary, as with the reference's atomicAdd append
+ * (ParticleSimulation.cu:250): each particle's edges are placed by one atomic
+ * in the selection pass itself. */
 int cf_proximity_vertices_device(cf_world* w, float distance, int max_conn, const cf_color* colors, int n_colors,
                                  float* vertices, int cap_vertices, int* vertex_count);
 

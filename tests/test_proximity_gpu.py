@@ -8,6 +8,7 @@ import pytest
 
 import oracle
 from cellflow_gb300 import inputs
+from cellflow_gb300._lib import CellFlowError
 from cellflow_gb300.world import ParticleSimulation
 from tests.parity import edge_set
 
@@ -70,7 +71,9 @@ def test_capacity_error(cflib):
 
 
 def test_vertices_layout(cflib):
-    """Vertex buffer in the reference's format: (x, y, z, r, g, b) for i then j, colour of i's type."""
+    """Vertex buffer in the reference's format: (x, y, z, r, g, b) for i then j, colour of i's type.
+    The edges' order in the buffer is arbitrary (as the reference's atomicAdd append), so the
+    vertex pairs are compared with the edge list's as sorted rows."""
     import torch
 
     n, T = 4000, 3
@@ -84,10 +87,29 @@ def test_vertices_layout(cflib):
     sim.close()
     assert count == 2 * len(edges)
     cols = np.asarray(colors, np.float32)
-    assert np.array_equal(v[0::2, :3], pos[edges[:, 0]])
-    assert np.array_equal(v[1::2, :3], pos[edges[:, 1]])
-    assert np.array_equal(v[0::2, 3:], cols[types[edges[:, 0]] % T])
-    assert np.array_equal(v[1::2, 3:], cols[types[edges[:, 0]] % T])
+    want = np.concatenate([pos[edges[:, 0]], cols[types[edges[:, 0]] % T], pos[edges[:, 1]],
+                           cols[types[edges[:, 0]] % T]], axis=1)
+    got = np.concatenate([v[0::2], v[1::2]], axis=1)
+    order = lambda a: a[np.lexsort(a.T[::-1])]
+    assert np.array_equal(order(got), order(want))
+
+
+def test_vertices_capacity(cflib):
+    """A vertex buffer too small for the edges gets CF_ERR_CAPACITY (the vertices that fit
+    are written, none past the buffer)."""
+    import torch
+
+    from cellflow_gb300._lib import CF_ERR_CAPACITY
+
+    n, T = 4000, 3
+    sim, pos, types = world(n, T, seed=8)
+    edges = sim.proximity_edges(0.1, 5)
+    colors = [(0.9, 0.1, 0.2), (0.1, 0.8, 0.3), (0.2, 0.3, 0.9)]
+    buf = torch.zeros((8, 6), dtype=torch.float32, device="cuda")
+    with pytest.raises(CellFlowError) as e:
+        sim.proximity_vertices_device(0.1, 5, colors, buf.data_ptr(), 8)
+    assert e.value.code == CF_ERR_CAPACITY
+    sim.close()
 
 
 def test_full_size_edges(cflib):
