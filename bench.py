@@ -951,9 +951,10 @@ def proximity_timing(sim, w, stream, calls):
         "value": edges / dev_s, "unit": "edges/s", "ms_per_call": dev_s * 1e3,
         "roofline": {"bound": "hbm", "achieved": prox_bytes / dev_s / 1e9, "peak": peaks.get("hbm_gbs"),
                      "unit": "GB/s", "frac": prox_bytes / dev_s / 1e9 / peaks.get("hbm_gbs", 6800.0),
-                     "work_model": "16 B/particle + 8 B/edge per call (the call is latency-bound: ~10 small "
-                                   "kernels and a count read-back)"},
-        "path": "cf_proximity_vertices_device (device VBO, count read back; synchronising, as the reference)",
+                     "work_model": "16 B/particle + 8 B/edge per call (the call is latency-bound: the proximity "
+                                   "grid's cell list, a selection pass that writes the vertices, a count "
+                                   "read-back)"},
+        "path": "cf_proximity_vertices_device (device VBO written by the selection pass in arbitrary edge order, as the reference's atomicAdd append; count read back; synchronising, as the reference)",
         "host_edges": {"value": len(host_edges) / host_s, "unit": "edges/s", "ms_per_call": host_s * 1e3,
                        "path": "cf_proximity_edges (int32 pairs into host memory)"},
     }
