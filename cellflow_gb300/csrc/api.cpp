@@ -365,8 +365,6 @@ int ensure_out(cf_world* w, size_t entries)
     return CF_OK;
 }
 
-// The colours of a vertex call, one per type, into the world's fixed colour
-// array (ordered on the stream before the kernel that reads them).
 // The per-type colours as the emit kernels' by-value table.
 ColorTable color_table(const cf_world* w, const cf_color* colors)
 {
@@ -1936,16 +1934,22 @@ int cf_proximity_edges(cf_world* w, float distance, int max_conn, int32_t* edges
     if (cap < 0 || (cap > 0 && !edges)) return fail(CF_ERR_INVALID, "bad edge buffer");
     rc = proximity_enqueue(w, distance, max_conn);
     if (rc) return rc;
+    // the edges go to the staging buffer right behind the selection, sized for the most
+    // a call can find (max_conn per particle, at most the caller's capacity), so the
+    // count and the edges arrive with one synchronisation; only the copy follows it
+    const int staged = (int)std::min<size_t>((size_t)cap, (size_t)w->n * (size_t)max_conn);
+    if (staged > 0) {
+        rc = ensure_out(w, 2 * (size_t)staged);
+        if (rc) return rc;
+        CF_CUDA(launch_proximity_emit_edges(w->s.prox_slots, w->s.prox_count, w->n, max_conn, w->s.out_idx, staged,
+                                            w->stream));
+    }
     rc = sync_and_check(w);
     if (rc) return rc;
     const uint32_t total = (uint32_t)w->host_words[1];
     if (n_edges) *n_edges = (int)total;
     const int write = (int)std::min<uint32_t>(total, (uint32_t)cap);
     if (write > 0) {
-        rc = ensure_out(w, 2 * (size_t)write);
-        if (rc) return rc;
-        CF_CUDA(launch_proximity_emit_edges(w->s.prox_slots, w->s.prox_count, w->n, max_conn, w->s.out_idx, write,
-                                            w->stream));
         rc = copy_out(w, edges, 2 * (size_t)write);
         if (rc) return rc;
     }
