@@ -30,9 +30,10 @@
 //     warp-uniform trip count from the filter's per-lane hit counts), the
 //     contracted distance of the displacement; pairs below a second bound
 //     (<= the exact test for every pair) interact for certain, and only the
-//     rare pairs between the two
-//     bounds (a band ~1e-6 wide) take the reference's exact test on the
-//     unshifted coordinates.  Interacting pairs add their force term.  In
+//     rare pairs between the two bounds (a band ~1e-6 wide) take the
+//     reference's exact test on the unshifted coordinates, in the trips where
+//     a warp vote finds one (written inline, its instructions ran predicated
+//     for every pair).  Interacting pairs add their force term.  In
 //     the lane-paired variant the lanes are sorted by hit count and paired
 //     busiest with idlest; the idler lane of a pair, after its own hits,
 //     walks the top part of its partner's with its partner's home and hands
